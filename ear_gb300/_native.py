@@ -1,0 +1,136 @@
+"""ctypes view of the C ABI declared in include/ear_gb300.h.
+
+The structures below mirror the header field for field.  ``lib()`` loads
+``ear_gb300/lib/libear_gb300.so`` (built in-tree by ``ear_gb300.build``)
+and raises if it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libear_gb300.so"
+
+EAR_OK = 0
+EAR_ERR_INVALID_ARG = 1
+EAR_ERR_OUT_OF_MEMORY = 2
+EAR_ERR_CUDA = 3
+EAR_ERR_DEVICE_BUDGET = 4
+EAR_ERR_STATE = 5
+EAR_ERR_UNSUPPORTED = 6
+
+EAR_FLAG_EXACT = 0x1
+EAR_FLAG_RAW = 0x2
+EAR_FLAG_NO_DIRECT = 0x4
+
+EAR_REFERENCE_MAX_BOUNCES = 999
+EAR_REFERENCE_CUTOFF = 1e-8
+SAMPLE_RATE = 44100
+
+F3 = C.c_float * 3
+
+
+class EarMaterial(C.Structure):
+    _fields_ = [("reflection", F3), ("refraction", F3), ("specularity", F3),
+                ("has_refraction", C.c_int32), ("has_specularity", C.c_int32)]
+
+
+class EarSceneDesc(C.Structure):
+    _fields_ = [("num_triangles", C.c_int64), ("vertices", C.POINTER(C.c_float)),
+                ("material_ids", C.POINTER(C.c_int32)), ("num_materials", C.c_int32),
+                ("materials", C.POINTER(EarMaterial)), ("device", C.c_int32)]
+
+
+class EarBvhOpts(C.Structure):
+    _fields_ = [("box_pad", C.c_float), ("reserved", C.c_int32 * 7)]
+
+
+class EarRecorder(C.Structure):
+    _fields_ = [("channels", C.c_int32), ("location", F3), ("right_ear", F3),
+                ("head_size", C.c_float), ("head_absorption", F3)]
+
+
+class EarSource(C.Structure):
+    _fields_ = [("location", F3), ("gain", C.c_float), ("num_emitter_triangles", C.c_int64),
+                ("emitter_vertices", C.POINTER(C.c_float))]
+
+
+class EarRenderParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("context", C.c_uint32), ("bands_mask", C.c_uint32),
+                ("num_rays", C.c_uint64), ("max_bounces", C.c_int32), ("num_bins", C.c_int32),
+                ("cutoff", C.c_double), ("air_absorption", F3), ("dry_level", C.c_float),
+                ("flags", C.c_uint32), ("reserved0", C.c_int32), ("stream", C.c_void_p)]
+
+
+class EarRenderStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("segments", C.c_uint64), ("shadow_queries", C.c_uint64),
+                ("contributions", C.c_uint64), ("sampler_overflows", C.c_uint64),
+                ("kernel_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class EarHistograms(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("first_sample", C.c_void_p), ("last_sample", C.c_void_p),
+                ("on_device", C.c_int32), ("reserved0", C.c_int32)]
+
+
+# Every exported symbol of include/ear_gb300.h with its ctypes signature.
+SIGNATURES = {
+    "ear_last_error": (C.c_char_p, []),
+    "ear_version": (C.c_char_p, []),
+    "ear_abi_version": (C.c_int32, []),
+    "ear_scene_create": (C.c_int, [C.POINTER(EarSceneDesc), C.POINTER(C.c_void_p)]),
+    "ear_scene_build_bvh": (C.c_int, [C.c_void_p, C.POINTER(EarBvhOpts)]),
+    "ear_scene_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int64)]),
+    "ear_scene_destroy": (None, [C.c_void_p]),
+    "ear_num_tracks": (C.c_int32, [C.POINTER(EarRecorder), C.c_int32]),
+    "ear_render": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder), C.c_int32,
+                             C.POINTER(EarRenderParams), C.POINTER(EarHistograms),
+                             C.POINTER(EarRenderStats)]),
+    "ear_trace_debug": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
+                                  C.c_int32, C.POINTER(EarRenderParams), C.c_int32, C.c_int32,
+                                  C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ear_track_power": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),
+    "ear_track_maximum": (C.c_float, [C.c_void_p, C.c_int32, C.c_int32]),
+    "ear_track_multiply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),
+    "ear_track_length": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float]),
+    "ear_track_t60": (C.c_float, [C.c_void_p, C.c_int32, C.c_int32]),
+    "ear_statistical_t60": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(EarMaterial),
+                                      C.c_float, C.c_void_p]),
+}
+
+_LIB = None
+
+
+class EarError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ear status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """Load the sm_103a library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -m ear_gb300.build` "
+                "(the CUDA path has no fallback)")
+        mode = getattr(os, "RTLD_GLOBAL", 0)
+        L = C.CDLL(str(LIB_PATH), mode=mode)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(status: int) -> None:
+    if status != EAR_OK:
+        msg = lib().ear_last_error()
+        raise EarError(status, msg.decode() if msg else "")

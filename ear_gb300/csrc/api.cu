@@ -1,0 +1,589 @@
+// api.cu -- implementation of the C ABI in include/ear_gb300.h.
+//
+// Host side of the drop-in boundary: validates arguments, derives the
+// per-material and per-recorder constants exactly as the reference's
+// constructors do (src/Material.cpp:26-72, src/StereoRecorder.cpp:53-57),
+// owns the device buffers of a scene, launches the trace kernels and runs
+// the end-of-render steps of Scene::Render (src/Scene.cpp:286-316).
+// Host code in this file is compiled with -ffp-contract=off.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/ear_gb300.h"
+#include "ear_internal.h"
+
+using namespace ear;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+ear_status fail(ear_status st, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return st;
+}
+
+#define CU(x)                                                                             \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,  \
+                  "%s: %s", #x, cudaGetErrorString(e_));                                  \
+  } while (0)
+
+constexpr int kInitialFirstSample = 3 * 44100 - 1;
+
+// Material::Material (src/Material.cpp:26-72) and Material::Bounce
+// (src/Material.cpp:76-83), per band.
+bool derive_material(const ear_material& m, DevMaterial* o) {
+  o->always_reflect = 0;
+  for (int i = 0; i < 3; ++i) {
+    float a = 1.0f;
+    a -= m.reflection[i] - 1e-9f;
+    if (m.has_refraction) a -= m.refraction[i] - 1e-9f;
+    if (a < 0.0f) return false;
+    o->survival[i] = 1.0f - a;
+    const float fl = m.reflection[i];
+    const float fr = m.has_refraction ? m.refraction[i] : 0.0f;
+    if ((double)fl < 0.0001 && (double)fr < 0.0001) o->always_reflect |= 1u << i;
+    o->p_reflect[i] = fl / (fl + fr);
+    o->spec[i] = m.has_specularity ? m.specularity[i] : 0.0f;
+  }
+  return true;
+}
+
+template <typename T>
+cudaError_t grow(T** p, size_t* cap, size_t n) {
+  if (n <= *cap && *p) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+__global__ void k_init_first_last(int2* fl, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) fl[i] = make_int2(kInitialFirstSample, 0);
+}
+
+// FloatBuffer::Multiply over [first_sample, real_length) of every traced
+// (track, band) row (src/Recorder.cpp:85-89).
+__global__ void k_scale(float* hist, int stride, int nb, int rows, const int2* fl, uint32_t bands,
+                        float f) {
+  const int row = blockIdx.y;
+  if (row >= rows || !((bands >> (row % 3)) & 1u)) return;
+  const int2 r = fl[row];
+  const int hi = r.y < nb ? r.y : nb;
+  float* h = hist + (size_t)row * stride;
+  for (int i = r.x + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
+    h[i] *= f;
+}
+
+}  // namespace
+
+struct ear_scene {
+  int device = 0;
+  DeviceScene ds;
+  int num_mats = 0;
+  DevMaterial* mats = nullptr;
+  bool bvh = false;
+  int sm_count = 0;
+  // render scratch, grown on demand and reused
+  float* hist = nullptr;
+  size_t hist_cap = 0;
+  int2* fl = nullptr;
+  size_t fl_cap = 0;
+  unsigned long long* counters = nullptr;
+  size_t counters_cap = 0;
+  int* err = nullptr;
+  size_t err_cap = 0;
+  DevRecorder* recs = nullptr;
+  size_t recs_cap = 0;
+  float4* emitter = nullptr;
+  size_t emitter_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+extern "C" {
+
+const char* ear_last_error(void) { return g_err; }
+const char* ear_version(void) { return "ear_gb300 0.1 (sm_103a)"; }
+int32_t ear_abi_version(void) { return EAR_ABI_VERSION; }
+
+int32_t ear_num_tracks(const ear_recorder* recorders, int32_t num_recorders) {
+  int32_t n = 0;
+  for (int32_t i = 0; i < num_recorders; ++i) n += recorders[i].channels == 2 ? 2 : 1;
+  return n;
+}
+
+ear_status ear_scene_create(const ear_scene_desc* desc, ear_scene** out) {
+  g_err[0] = 0;
+  if (!desc || !out) return fail(EAR_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (desc->num_triangles < 0 || (desc->num_triangles > 0 && (!desc->vertices || !desc->material_ids)))
+    return fail(EAR_ERR_INVALID_ARG, "bad triangle arrays");
+  if (desc->num_triangles >= (int64_t)kLeafStartMask)
+    return fail(EAR_ERR_INVALID_ARG, "at most %d triangles per scene", kLeafStartMask - 1);
+  if (desc->num_materials < 0 || (desc->num_materials > 0 && !desc->materials))
+    return fail(EAR_ERR_INVALID_ARG, "bad material array");
+  if (desc->num_materials > 4096) return fail(EAR_ERR_INVALID_ARG, "at most 4096 materials");
+  std::vector<DevMaterial> mats((size_t)desc->num_materials);
+  for (int i = 0; i < desc->num_materials; ++i)
+    if (!derive_material(desc->materials[i], &mats[(size_t)i]))
+      return fail(EAR_ERR_INVALID_ARG, "Invalid material settings (material %d)", i);
+  for (int64_t i = 0; i < desc->num_triangles; ++i) {
+    const int m = desc->material_ids[i];
+    if (m < 0 || m >= desc->num_materials)
+      return fail(EAR_ERR_INVALID_ARG, "material id %d out of range at triangle %lld", m,
+                  (long long)i);
+  }
+  for (int64_t i = 0; i < desc->num_triangles * 9; ++i)
+    if (!std::isfinite(desc->vertices[i]))
+      return fail(EAR_ERR_INVALID_ARG, "non-finite vertex coordinate at triangle %lld",
+                  (long long)(i / 9));
+  CU(cudaSetDevice(desc->device));
+  ear_scene* s = new ear_scene();
+  s->device = desc->device;
+  s->ds.num_tris = desc->num_triangles;
+  s->num_mats = desc->num_materials;
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  cudaError_t e = cudaSuccess;
+  const size_t nt = (size_t)desc->num_triangles;
+  if (nt) {
+    e = cudaMalloc(&s->ds.vertices, sizeof(float) * 9 * nt);
+    if (e == cudaSuccess) e = cudaMalloc(&s->ds.mat_ids, sizeof(int32_t) * nt);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(s->ds.vertices, desc->vertices, sizeof(float) * 9 * nt, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(s->ds.mat_ids, desc->material_ids, sizeof(int32_t) * nt, cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&s->mats, sizeof(DevMaterial) * std::max<size_t>(mats.size(), 1));
+  if (e == cudaSuccess && !mats.empty())
+    e = cudaMemcpy(s->mats, mats.data(), sizeof(DevMaterial) * mats.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+  if (e != cudaSuccess) {
+    ear_scene_destroy(s);
+    return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
+                "scene upload: %s", cudaGetErrorString(e));
+  }
+  *out = s;
+  return EAR_OK;
+}
+
+ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
+  g_err[0] = 0;
+  if (!s) return fail(EAR_ERR_INVALID_ARG, "null scene");
+  CU(cudaSetDevice(s->device));
+  char msg[256] = "";
+  const float pad = opts ? opts->box_pad : -1.0f;
+  cudaError_t e = build_lbvh(s->ds, pad, 0, msg, sizeof msg);
+  if (e != cudaSuccess) {
+    s->bvh = false;
+    return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
+                "LBVH build: %s", msg[0] ? msg : cudaGetErrorString(e));
+  }
+  s->bvh = true;
+  return EAR_OK;
+}
+
+ear_status ear_scene_info(const ear_scene* s, int64_t* num_triangles, int64_t* num_nodes,
+                          int32_t* max_depth, float* box_pad, int64_t* device_bytes) {
+  if (!s) return fail(EAR_ERR_INVALID_ARG, "null scene");
+  if (num_triangles) *num_triangles = s->ds.num_tris;
+  if (num_nodes) *num_nodes = s->ds.num_nodes;
+  if (max_depth) *max_depth = s->ds.max_depth;
+  if (box_pad) *box_pad = s->ds.box_pad;
+  if (device_bytes)
+    *device_bytes = (int64_t)(s->ds.num_nodes * sizeof(Node) + s->ds.num_tris * (48 + 16 + 36 + 4));
+  return EAR_OK;
+}
+
+void ear_scene_destroy(ear_scene* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  cudaFree(s->ds.nodes);
+  cudaFree(s->ds.tris);
+  cudaFree(s->ds.nrm);
+  cudaFree(s->ds.vertices);
+  cudaFree(s->ds.mat_ids);
+  cudaFree(s->mats);
+  cudaFree(s->hist);
+  cudaFree(s->fl);
+  cudaFree(s->counters);
+  cudaFree(s->err);
+  cudaFree(s->recs);
+  cudaFree(s->emitter);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  delete s;
+}
+
+}  // extern "C"
+
+namespace {
+
+struct Prepared {
+  TraceArgs a;
+  int num_tracks;
+  size_t smem;
+  int grid;
+  const TraceOps* ops;
+};
+
+ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs, int32_t nrec,
+                   const ear_render_params* p, uint32_t bands_mask, Prepared* out) {
+  if (!s || !src || !p || (nrec > 0 && !recs)) return fail(EAR_ERR_INVALID_ARG, "null argument");
+  if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
+  if (nrec < 0 || nrec > kMaxRecorders)
+    return fail(EAR_ERR_INVALID_ARG, "between 0 and %d recorders", kMaxRecorders);
+  if (p->num_bins <= 0 || p->num_bins > (1 << 30)) return fail(EAR_ERR_INVALID_ARG, "bad num_bins");
+  if (bands_mask == 0 || (bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
+  if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
+  if (p->num_rays > (1ull << 47)) return fail(EAR_ERR_INVALID_ARG, "num_rays above 2^47");
+  if (src->num_emitter_triangles < 0 || (src->num_emitter_triangles > 0 && !src->emitter_vertices))
+    return fail(EAR_ERR_INVALID_ARG, "bad emitter triangles");
+  std::vector<DevRecorder> dr((size_t)nrec);
+  int tracks = 0;
+  for (int i = 0; i < nrec; ++i) {
+    const ear_recorder& r = recs[i];
+    if (r.channels != 1 && r.channels != 2)
+      return fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
+    DevRecorder& d = dr[(size_t)i];
+    for (int k = 0; k < 3; ++k) {
+      d.loc[k] = r.location[k];
+      d.right[k] = r.right_ear[k];
+      // std::max(0.0f, powf(1.0f - h, 4)) (src/StereoRecorder.cpp:56)
+      const float h = powf_portable(1.0f - r.head_absorption[k], 4.0f);
+      d.habs[k] = (0.0f < h) ? h : 0.0f;
+    }
+    d.head_size = r.head_size;
+    d.channels = r.channels;
+    d.track0 = tracks;
+    tracks += r.channels;
+  }
+  TraceArgs& a = out->a;
+  std::memset(&a, 0, sizeof a);
+  const bool exact = (p->flags & EAR_FLAG_EXACT) != 0;
+  out->ops = exact ? &kTraceExact : &kTraceFast;
+  a.nodes = s->ds.nodes;
+  a.tris = s->ds.tris;
+  a.nrm = s->ds.nrm;
+  a.num_tris = (int)s->ds.num_tris;
+  a.num_nodes = (int)s->ds.num_nodes;
+  a.mats = s->mats;
+  a.num_mats = s->num_mats;
+  a.num_recs = nrec;
+  for (int k = 0; k < 3; ++k) a.src[k] = src->location[k];
+  a.k0 = (uint32_t)p->seed;
+  a.k1 = (uint32_t)(p->seed >> 32);
+  a.context = p->context;
+  int nb = 0;
+  for (int b = 0; b < 3; ++b) {
+    a.bands[b] = -1;
+    if (bands_mask & (1u << b)) a.bands[nb++] = b;
+    a.air[b] = 1.0f - p->air_absorption[b];
+  }
+  a.num_rays = p->num_rays;
+  a.num_items = p->num_rays * (uint64_t)nb;
+  a.max_bounces = p->max_bounces;
+  a.cutoff = p->cutoff;
+  a.box_pad = s->ds.box_pad;
+  a.num_bins = p->num_bins;
+  a.stride = (p->num_bins + 3) & ~3;
+  a.num_tracks = tracks;
+  a.traverse_budget = (int)std::min<int64_t>(4 * s->ds.num_nodes + 64, (int64_t)1 << 30);
+  a.dbg_band = -1;
+  out->num_tracks = tracks;
+
+  CU(cudaSetDevice(s->device));
+  CU(grow(&s->recs, &s->recs_cap, (size_t)std::max(nrec, 1)));
+  CU(grow(&s->fl, &s->fl_cap, (size_t)std::max(tracks * 3, 1)));
+  CU(grow(&s->counters, &s->counters_cap, (size_t)kNumCounters));
+  CU(grow(&s->err, &s->err_cap, (size_t)1));
+  CU(grow(&s->hist, &s->hist_cap, (size_t)std::max(tracks * 3, 1) * (size_t)a.stride));
+  a.recs = s->recs;
+  a.hist = s->hist;
+  a.first_last = s->fl;
+  a.counters = s->counters;
+  a.error_flag = s->err;
+  cudaStream_t st = (cudaStream_t)p->stream;
+  if (nrec) CU(cudaMemcpyAsync(s->recs, dr.data(), sizeof(DevRecorder) * nrec, cudaMemcpyHostToDevice, st));
+  // emitter: (a, area) (b, 0) (c, 0) (normal, 0) per triangle
+  if (src->num_emitter_triangles > 0) {
+    const int64_t ne = src->num_emitter_triangles;
+    if (ne > (1 << 24)) return fail(EAR_ERR_INVALID_ARG, "emitter too large");
+    std::vector<float4> em((size_t)ne * 4);
+    float total = 0.0f;
+    for (int64_t i = 0; i < ne; ++i) {
+      const float* v = src->emitter_vertices + 9 * i;
+      const V3 A = mk(v[0], v[1], v[2]), B = mk(v[3], v[4], v[5]), C = mk(v[6], v[7], v[8]);
+      const V3 nn = normalized(cross(sub(B, A), sub(C, A)));
+      // Triangle::calcArea: |edge(0) x edge(1)| / 2 (src/Triangle.cpp:26-30)
+      const float area = length(cross(sub(B, A), sub(C, B))) / 2.0f;
+      total += area;  // Mesh::Mesh (src/Mesh.cpp:90)
+      em[(size_t)i * 4 + 0] = make_float4(A.x, A.y, A.z, area);
+      em[(size_t)i * 4 + 1] = make_float4(B.x, B.y, B.z, 0.0f);
+      em[(size_t)i * 4 + 2] = make_float4(C.x, C.y, C.z, 0.0f);
+      em[(size_t)i * 4 + 3] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+    }
+    CU(grow(&s->emitter, &s->emitter_cap, em.size()));
+    CU(cudaMemcpyAsync(s->emitter, em.data(), sizeof(float4) * em.size(), cudaMemcpyHostToDevice, st));
+    a.emitter = s->emitter;
+    a.num_emitter = (int)ne;
+    a.emitter_total_area = total;
+  }
+  CU(cudaMemsetAsync(s->hist, 0, sizeof(float) * (size_t)std::max(tracks * 3, 1) * a.stride, st));
+  CU(cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * kNumCounters, st));
+  CU(cudaMemsetAsync(s->err, 0, sizeof(int), st));
+  if (tracks) {
+    k_init_first_last<<<(tracks * 3 + 127) / 128, 128, 0, st>>>(s->fl, tracks * 3);
+    CU(cudaGetLastError());
+  }
+  out->smem = sizeof(DevMaterial) * (size_t)s->num_mats + sizeof(int) * 2 * 3 * (size_t)tracks;
+  if (out->smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
+  int per_sm = 0;
+  CU(out->ops->occupancy(false, out->smem, &per_sm));
+  if (per_sm < 1) per_sm = 1;
+  out->grid = s->sm_count * per_sm;
+  return EAR_OK;
+}
+
+ear_status finish(ear_scene* s, const ear_render_params* p, const Prepared& pr, double* kernel_ms) {
+  cudaStream_t st = (cudaStream_t)p->stream;
+  CU(cudaStreamSynchronize(st));
+  int errflag = 0;
+  CU(cudaMemcpy(&errflag, s->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (kernel_ms) {
+    float ms = 0.0f;
+    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    *kernel_ms = ms;
+  }
+  if (errflag & kErrBudget)
+    return fail(EAR_ERR_DEVICE_BUDGET, "a BVH traversal exceeded its iteration budget");
+  return EAR_OK;
+}
+
+}  // namespace
+
+extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_recorder* recs,
+                                 int32_t nrec, const ear_render_params* p, ear_histograms* out,
+                                 ear_render_stats* stats) {
+  g_err[0] = 0;
+  if (!out || !out->data) return fail(EAR_ERR_INVALID_ARG, "null output");
+  if (!p) return fail(EAR_ERR_INVALID_ARG, "null params");
+  Prepared pr;
+  ear_status rc = prepare(s, src, recs, nrec, p, p->bands_mask, &pr);
+  if (rc != EAR_OK) return rc;
+  TraceArgs& a = pr.a;
+  cudaStream_t st = (cudaStream_t)p->stream;
+  CU(cudaEventRecord(s->ev0, st));
+  if (a.num_items > 0) CU(pr.ops->trace(a, pr.grid, pr.smem, false, st));
+  CU(cudaEventRecord(s->ev1, st));
+  const int rows = pr.num_tracks * 3;
+  if (!(p->flags & EAR_FLAG_RAW) && rows > 0) {
+    // src/Scene.cpp:286-316: Multiply(1/amount), direct sound, Multiply(gain^2).
+    // amount is a float incremented once per ray: exact to 2^24, then stuck.
+    const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
+    const float inv_amount = 1.0f / amount;
+    const float gain2 = src->gain * src->gain;
+    const dim3 grid((unsigned)std::min(1024, (a.num_bins + 255) / 256), (unsigned)rows);
+    k_scale<<<grid, 256, 0, st>>>(a.hist, a.stride, a.num_bins, rows, a.first_last, p->bands_mask,
+                                  inv_amount);
+    CU(cudaGetLastError());
+    if (src->num_emitter_triangles <= 0 && !(p->flags & EAR_FLAG_NO_DIRECT))
+      CU(pr.ops->direct(a, p->dry_level, st));
+    k_scale<<<grid, 256, 0, st>>>(a.hist, a.stride, a.num_bins, rows, a.first_last, p->bands_mask,
+                                  gain2);
+    CU(cudaGetLastError());
+  }
+  if (rows > 0) {
+    const cudaMemcpyKind kind = out->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    CU(cudaMemcpy2DAsync(out->data, sizeof(float) * a.num_bins, a.hist, sizeof(float) * a.stride,
+                         sizeof(float) * a.num_bins, (size_t)rows, kind, st));
+  }
+  std::vector<int2> fl((size_t)std::max(rows, 1));
+  if (rows > 0) CU(cudaMemcpyAsync(fl.data(), a.first_last, sizeof(int2) * rows, cudaMemcpyDeviceToHost, st));
+  unsigned long long cnt[kNumCounters];
+  CU(cudaMemcpyAsync(cnt, a.counters, sizeof cnt, cudaMemcpyDeviceToHost, st));
+  double ms = 0.0;
+  rc = finish(s, p, pr, &ms);
+  if (rc != EAR_OK) return rc;
+  if (out->first_sample || out->last_sample) {
+    std::vector<int32_t> f((size_t)std::max(rows, 1)), l((size_t)std::max(rows, 1));
+    for (int i = 0; i < rows; ++i) {
+      f[(size_t)i] = std::min(fl[(size_t)i].x, a.num_bins);
+      l[(size_t)i] = std::min(fl[(size_t)i].y, a.num_bins);
+    }
+    const cudaMemcpyKind k2 = out->on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+    if (out->first_sample && rows) CU(cudaMemcpy(out->first_sample, f.data(), sizeof(int32_t) * rows, k2));
+    if (out->last_sample && rows) CU(cudaMemcpy(out->last_sample, l.data(), sizeof(int32_t) * rows, k2));
+  }
+  if (stats) {
+    stats->rays = std::min<unsigned long long>(cnt[kWork], a.num_items);
+    stats->segments = cnt[kSegments];
+    stats->shadow_queries = cnt[kShadow];
+    stats->contributions = cnt[kContrib];
+    stats->sampler_overflows = cnt[kOverflow];
+    stats->kernel_ms = ms;
+  }
+  return EAR_OK;
+}
+
+extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
+                                      const ear_recorder* recs, int32_t nrec,
+                                      const ear_render_params* p, int32_t band, int32_t max_record,
+                                      int32_t* hit_tri, uint8_t* bounce_type, uint32_t* visible) {
+  g_err[0] = 0;
+  if (!p || !hit_tri || !bounce_type || !visible || max_record <= 0 || band < 0 || band > 2)
+    return fail(EAR_ERR_INVALID_ARG, "bad debug arguments");
+  Prepared pr;
+  ear_status rc = prepare(s, src, recs, nrec, p, 1u << band, &pr);
+  if (rc != EAR_OK) return rc;
+  TraceArgs& a = pr.a;
+  const size_t n = (size_t)p->num_rays * (size_t)max_record;
+  if (n > ((size_t)1 << 31)) return fail(EAR_ERR_INVALID_ARG, "debug record too large");
+  int32_t* dh = nullptr;
+  uint8_t* db = nullptr;
+  uint32_t* dv = nullptr;
+  cudaStream_t st = (cudaStream_t)p->stream;
+  std::vector<int32_t> init(n, -2);
+  cudaError_t e = cudaMalloc(&dh, sizeof(int32_t) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&db, std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&dv, sizeof(uint32_t) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(dh, init.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n) e = cudaMemsetAsync(db, 0, n, st);
+  if (e == cudaSuccess && n) e = cudaMemsetAsync(dv, 0, sizeof(uint32_t) * n, st);
+  if (e == cudaSuccess) {
+    a.dbg_band = band;
+    a.dbg_rays = (int64_t)p->num_rays;
+    a.dbg_max_record = max_record;
+    a.dbg_hit = dh;
+    a.dbg_bt = db;
+    a.dbg_vis = dv;
+    e = cudaEventRecord(s->ev0, st);
+    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, true, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(hit_tri, dh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(bounce_type, db, n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(visible, dv, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  cudaFree(dh);
+  cudaFree(db);
+  cudaFree(dv);
+  if (e != cudaSuccess) return fail(EAR_ERR_CUDA, "debug trace: %s", cudaGetErrorString(e));
+  return finish(s, p, pr, nullptr);
+}
+
+// ------------------------------------------------- FloatBuffer post-process
+extern "C" {
+
+ear_status ear_track_power(float* data, int32_t first, int32_t last, float a) {
+  if (!data && last > first) return fail(EAR_ERR_INVALID_ARG, "null track");
+  for (int32_t i = first; i < last; ++i) {
+    const float f = std::pow(std::fabs(data[i]), a);
+    data[i] = data[i] < 0 ? (f * -1.0f) : f;
+  }
+  return EAR_OK;
+}
+
+float ear_track_maximum(const float* data, int32_t first, int32_t last) {
+  float x = 0.0f;
+  for (int32_t i = first; i < last; ++i) {
+    const float a = std::fabs(data[i]);
+    if (a > x) x = a;
+  }
+  return x;
+}
+
+ear_status ear_track_multiply(float* data, int32_t first, int32_t last, float f) {
+  if (!data && last > first) return fail(EAR_ERR_INVALID_ARG, "null track");
+  for (int32_t i = first; i < last; ++i) data[i] *= f;
+  return EAR_OK;
+}
+
+int32_t ear_track_length(const float* data, int32_t capacity, int32_t first, int32_t last,
+                         float tresh) {
+  if (tresh < 0.0f) return last;
+  int32_t mx = 0;
+  for (int32_t i = first; i < capacity; ++i)
+    if (std::fabs(data[i]) >= tresh) mx = i;
+  return mx + 1;
+}
+
+float ear_track_t60(const float* data, int32_t first, int32_t last) {
+  const float attenuation_gain = std::pow(10.0f, 60.0f / 20.0f);
+  float min_gain = 0.0f;
+  int last_significant_offset = 0, direct_sound_offset = 0;
+  float previous_sample = -1.0f;
+  bool inside_indirect_lobe = false;
+  for (int32_t j = first; j < last; ++j) {
+    const float sample = data[j];
+    if (inside_indirect_lobe) {
+      if (sample > min_gain) last_significant_offset = j;
+    } else if (sample < previous_sample) {
+      inside_indirect_lobe = true;
+      min_gain = previous_sample / attenuation_gain;
+      direct_sound_offset = j;
+    }
+    previous_sample = sample;
+  }
+  return (float)(last_significant_offset - direct_sound_offset) / 44100.0f;
+}
+
+ear_status ear_statistical_t60(const float* vertices, const int64_t* block_triangles,
+                               int32_t num_blocks, const ear_material* first_block_material,
+                               float air_absorption_mid, float* out) {
+  g_err[0] = 0;
+  if (!vertices || !block_triangles || num_blocks <= 0 || !first_block_material || !out)
+    return fail(EAR_ERR_INVALID_ARG, "bad arguments");
+  DevMaterial m;
+  if (!derive_material(*first_block_material, &m))
+    return fail(EAR_ERR_INVALID_ARG, "Invalid material settings");
+  // Mesh::Mesh: absorption = 1 - absorption_coefficient[1] (src/Mesh.cpp:85)
+  const float absorption = 1.0f - m.survival[1];
+  float total_area = 0.0f, weighted = 0.0f, volume = 0.0f;
+  int64_t t = 0;
+  for (int32_t b = 0; b < num_blocks; ++b) {
+    float block_area = 0.0f;
+    for (int64_t i = 0; i < block_triangles[b]; ++i, ++t) {
+      const float* v = vertices + 9 * t;
+      const V3 p1 = mk(v[0], v[1], v[2]), p2 = mk(v[3], v[4], v[5]), p3 = mk(v[6], v[7], v[8]);
+      const float area = length(cross(sub(p2, p1), sub(p3, p2))) / 2.0f;
+      block_area += area;
+      if (b == 0) weighted += area * absorption;
+      // Triangle::SignedVolume (src/Triangle.cpp:55-67)
+      const float v321 = p3.x * p2.y * p1.z;
+      const float v231 = p2.x * p3.y * p1.z;
+      const float v312 = p3.x * p1.y * p2.z;
+      const float v132 = p1.x * p3.y * p2.z;
+      const float v213 = p2.x * p1.y * p3.z;
+      const float v123 = p1.x * p2.y * p3.z;
+      volume += (1.0f / 6.0f) * (-v321 + v231 + v312 - v132 - v213 + v123);
+    }
+    total_area += block_area;
+  }
+  const float V = volume, A = weighted, S = total_area, a = weighted / total_area;
+  const float mm = air_absorption_mid;
+  out[0] = V;
+  out[1] = S;
+  out[2] = A;
+  out[3] = 0.1611f * V / (A + 4.0f * mm * V);
+  out[4] = 0.1611f * V / (-S * std::log(1.0f - a) + 4.0f * mm * V);
+  return EAR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,346 @@
+// bvh_build.cu -- linear BVH built on the device.
+//
+// The reference has no acceleration structure (src/Scene.h:37-41): every
+// query loops over all triangles (src/Mesh.cpp:33-71).  This file builds a
+// binary LBVH (Karras, "Maximizing parallelism in the construction of BVHs,
+// octrees, and k-d trees", HPG 2012): 30-bit Morton codes of the box
+// centres, a device radix sort, one thread per internal node to find its
+// range and split, and a bottom-up refit with one atomic visit counter per
+// node.  Compiled with --fmad=false: the per-triangle edges and normals it
+// writes must equal the CPU restatement's bit for bit.
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include <stdio.h>
+
+#include "ear_internal.h"
+
+namespace ear {
+namespace {
+
+// float <-> order-preserving uint for atomicMin/atomicMax on floats
+__device__ __forceinline__ uint32_t ord(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float unord(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+#else
+  return u2f((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+#endif
+}
+
+// bounds[0..2] = min centre, [3..5] = max centre, [6] = max |coordinate|
+__global__ void k_tri_boxes(const float* __restrict__ v, int64_t n, float4* __restrict__ lo,
+                            float4* __restrict__ hi, uint32_t* __restrict__ bounds) {
+  __shared__ uint32_t sb[7];
+  if (threadIdx.x < 7) sb[threadIdx.x] = (threadIdx.x < 3) ? 0xffffffffu : 0u;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float* p = v + 9 * i;
+    float l[3], h[3];
+    float mabs = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+      const float x = p[a], y = p[3 + a], z = p[6 + a];
+      l[a] = fminf(fminf(x, y), z);
+      h[a] = fmaxf(fmaxf(x, y), z);
+      mabs = fmaxf(mabs, fmaxf(fabsf(l[a]), fabsf(h[a])));
+    }
+    lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+    hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
+    for (int a = 0; a < 3; ++a) {
+      const float c = 0.5f * l[a] + 0.5f * h[a];
+      atomicMin(&sb[a], ord(c));
+      atomicMax(&sb[3 + a], ord(c));
+    }
+    atomicMax(&sb[6], ord(mabs));
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) atomicMin(&bounds[threadIdx.x], sb[threadIdx.x]);
+  else if (threadIdx.x < 7) atomicMax(&bounds[threadIdx.x], sb[threadIdx.x]);
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+__global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, int64_t n,
+                         const uint32_t* __restrict__ bounds, uint32_t* __restrict__ codes,
+                         int32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 l = lo[i], h = hi[i];
+  const float c[3] = {0.5f * l.x + 0.5f * h.x, 0.5f * l.y + 0.5f * h.y, 0.5f * l.z + 0.5f * h.z};
+  uint32_t code = 0;
+  for (int a = 0; a < 3; ++a) {
+    const float mn = unord(bounds[a]), mx = unord(bounds[3 + a]);
+    const float ext = mx - mn;
+    float f = ext > 0.0f ? (c[a] - mn) / ext : 0.5f;
+    f = fminf(fmaxf(f * 1024.0f, 0.0f), 1023.0f);
+    code |= spread10((uint32_t)f) << (2 - a);
+  }
+  codes[i] = code;
+  idx[i] = (int32_t)i;
+}
+
+// Common-prefix length of the augmented keys (code, index).
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint32_t a = codes[i], b = codes[j];
+  if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+  return __clz(a ^ b);
+}
+
+// One thread per internal node (Karras 2012, Fig. 4).
+__global__ void k_karras(const uint32_t* __restrict__ codes, int n, Node* __restrict__ nodes,
+                         int32_t* __restrict__ leaf_parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta(codes, n, i, i + 1) - delta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta(codes, n, i, i - d);
+  int lmax = 2;
+  while (delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta(codes, n, i, j);
+  int s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int gamma = i + s * d + (d < 0 ? d : 0);
+  const int first = i < j ? i : j, last = i < j ? j : i;
+  int c0, c1;
+  if (first == gamma) {
+    c0 = ~gamma;
+    leaf_parent[gamma] = i;
+  } else {
+    c0 = gamma;
+    nodes[gamma].d.z = i;
+  }
+  if (last == gamma + 1) {
+    c1 = ~(gamma + 1);
+    leaf_parent[gamma + 1] = i;
+  } else {
+    c1 = gamma + 1;
+    nodes[gamma + 1].d.z = i;
+  }
+  nodes[i].d.x = c0;
+  nodes[i].d.y = c1;
+  if (i == 0) nodes[0].d.z = -1;
+}
+
+// Bottom-up refit: the second thread to reach a node merges its children.
+__global__ void k_refit(const float4* __restrict__ lo, const float4* __restrict__ hi,
+                        const int32_t* __restrict__ sorted_idx, const int32_t* __restrict__ leaf_parent,
+                        int n, float pad, Node* nodes, float4* node_lo, float4* node_hi,
+                        uint32_t* visits) {
+  const int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= n) return;
+  int p = leaf_parent[leaf];
+  while (p >= 0) {
+    __threadfence();
+    if (atomicAdd(&visits[p], 1u) == 0u) return;
+    __threadfence();
+    const int4 ch = __ldcg(&nodes[p].d);
+    float4 bl[2], bh[2];
+    const int c[2] = {ch.x, ch.y};
+    for (int k = 0; k < 2; ++k) {
+      if (c[k] < 0) {
+        const int t = sorted_idx[~c[k] & kLeafStartMask];
+        const float4 l = lo[t], h = hi[t];
+        bl[k] = make_float4(l.x - pad, l.y - pad, l.z - pad, 0.0f);
+        bh[k] = make_float4(h.x + pad, h.y + pad, h.z + pad, 0.0f);
+      } else {
+        bl[k] = __ldcg(&node_lo[c[k]]);
+        bh[k] = __ldcg(&node_hi[c[k]]);
+      }
+    }
+    Node& nd = nodes[p];
+    nd.a = make_float4(bl[0].x, bh[0].x, bl[0].y, bh[0].y);
+    nd.b = make_float4(bl[0].z, bh[0].z, bl[1].x, bh[1].x);
+    nd.c = make_float4(bl[1].y, bh[1].y, bl[1].z, bh[1].z);
+    node_lo[p] = make_float4(fminf(bl[0].x, bl[1].x), fminf(bl[0].y, bl[1].y),
+                             fminf(bl[0].z, bl[1].z), 0.0f);
+    node_hi[p] = make_float4(fmaxf(bh[0].x, bh[1].x), fmaxf(bh[0].y, bh[1].y),
+                             fmaxf(bh[0].z, bh[1].z), 0.0f);
+    p = __ldcg(&nodes[p].d.z);
+  }
+}
+
+// Depth of every leaf (internal nodes on its root path + 1).
+__global__ void k_depth(const int32_t* __restrict__ leaf_parent, int n, const Node* __restrict__ nodes,
+                        int* max_depth) {
+  const int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= n) return;
+  int depth = 1;
+  for (int p = leaf_parent[leaf]; p >= 0 && depth < 4096; p = nodes[p].d.z) ++depth;
+  atomicMax(max_depth, depth);
+}
+
+// Gather triangles into leaf order with edges, normals and materials.
+__global__ void k_gather(const float* __restrict__ v, const int32_t* __restrict__ mat_ids,
+                         const int32_t* __restrict__ sorted_idx, int n, float4* __restrict__ tris,
+                         float4* __restrict__ nrm) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int t = sorted_idx[j];
+  const float* p = v + 9 * (int64_t)t;
+  const V3 a = mk(p[0], p[1], p[2]), b = mk(p[3], p[4], p[5]), c = mk(p[6], p[7], p[8]);
+  const V3 e1 = sub(b, a), e2 = sub(c, a);
+  const V3 nn = normalized(cross(e1, e2));
+  tris[3 * j + 0] = make_float4(a.x, a.y, a.z, __int_as_float(t));
+  tris[3 * j + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+  tris[3 * j + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+  nrm[j] = make_float4(nn.x, nn.y, nn.z, __int_as_float(mat_ids[t]));
+}
+
+// Single-triangle scene: a root whose two children are the same leaf.
+__global__ void k_single(const float4* __restrict__ lo, const float4* __restrict__ hi, float pad,
+                         Node* nodes) {
+  const float4 l = lo[0], h = hi[0];
+  const float lx = l.x - pad, ly = l.y - pad, lz = l.z - pad;
+  const float hx = h.x + pad, hy = h.y + pad, hz = h.z + pad;
+  nodes[0].a = make_float4(lx, hx, ly, hy);
+  nodes[0].b = make_float4(lz, hz, lx, hx);
+  nodes[0].c = make_float4(ly, hy, lz, hz);
+  nodes[0].d = make_int4(~0, ~0, -1, 0);
+}
+
+#define CK(x)                                                              \
+  do {                                                                     \
+    cudaError_t e_ = (x);                                                  \
+    if (e_ != cudaSuccess) {                                               \
+      snprintf(err, errlen, "%s failed: %s", #x, cudaGetErrorString(e_));  \
+      rc = e_;                                                             \
+      goto done;                                                           \
+    }                                                                      \
+  } while (0)
+
+}  // namespace
+
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char* err,
+                       size_t errlen) {
+  const int64_t n64 = s.num_tris;
+  cudaError_t rc = cudaSuccess;
+  err[0] = 0;
+  if (n64 >= (int64_t)kLeafStartMask) {
+    snprintf(err, errlen, "too many triangles for one scene (%lld)", (long long)n64);
+    return cudaErrorInvalidValue;
+  }
+  const int n = (int)n64;
+  float4 *lo = nullptr, *hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
+  uint32_t *bounds = nullptr, *codes = nullptr, *codes2 = nullptr, *visits = nullptr;
+  int32_t *idx = nullptr, *idx2 = nullptr, *leaf_parent = nullptr;
+  int* dmax = nullptr;
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  uint32_t hb[7];
+  const int nn = n > 1 ? n - 1 : 1;
+  const int B = 256;
+  const int G = (n + B - 1) / B;
+  int depth = 1;
+
+  if (s.nodes) cudaFree(s.nodes);
+  if (s.tris) cudaFree(s.tris);
+  if (s.nrm) cudaFree(s.nrm);
+  s.nodes = nullptr;
+  s.tris = nullptr;
+  s.nrm = nullptr;
+  s.num_nodes = 0;
+  if (n == 0) {
+    s.max_depth = 0;
+    s.box_pad = 0.0f;
+    return cudaSuccess;
+  }
+  CK(cudaMalloc(&lo, sizeof(float4) * n));
+  CK(cudaMalloc(&hi, sizeof(float4) * n));
+  CK(cudaMalloc(&bounds, sizeof(uint32_t) * 8));
+  CK(cudaMalloc(&codes, sizeof(uint32_t) * n));
+  CK(cudaMalloc(&codes2, sizeof(uint32_t) * n));
+  CK(cudaMalloc(&idx, sizeof(int32_t) * n));
+  CK(cudaMalloc(&idx2, sizeof(int32_t) * n));
+  CK(cudaMalloc(&leaf_parent, sizeof(int32_t) * n));
+  CK(cudaMalloc(&node_lo, sizeof(float4) * nn));
+  CK(cudaMalloc(&node_hi, sizeof(float4) * nn));
+  CK(cudaMalloc(&visits, sizeof(uint32_t) * nn));
+  CK(cudaMalloc(&dmax, sizeof(int)));
+  CK(cudaMalloc(&s.nodes, sizeof(Node) * nn));
+  CK(cudaMalloc(&s.tris, sizeof(float4) * 3 * (size_t)n));
+  CK(cudaMalloc(&s.nrm, sizeof(float4) * (size_t)n));
+  {
+    const uint32_t init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0u};
+    CK(cudaMemcpyAsync(bounds, init, sizeof init, cudaMemcpyHostToDevice, stream));
+  }
+  CK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nn, stream));
+  CK(cudaMemsetAsync(dmax, 0, sizeof(int), stream));
+  CK(cudaMemsetAsync(s.nodes, 0, sizeof(Node) * nn, stream));
+  k_tri_boxes<<<G, B, 0, stream>>>(s.vertices, n, lo, hi, bounds);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(hb, bounds, sizeof(uint32_t) * 7, cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  {
+    const float max_abs = unord(hb[6]);
+    s.box_pad = box_pad >= 0.0f ? box_pad : max_abs * (1.0f / 4096.0f) + 1e-5f;
+  }
+  if (n == 1) {
+    k_single<<<1, 1, 0, stream>>>(lo, hi, s.box_pad, s.nodes);
+    CK(cudaGetLastError());
+    {
+      const int32_t zero = 0;
+      CK(cudaMemcpyAsync(idx2, &zero, sizeof zero, cudaMemcpyHostToDevice, stream));
+    }
+    depth = 1;
+  } else {
+    k_morton<<<G, B, 0, stream>>>(lo, hi, n, bounds, codes, idx);
+    CK(cudaGetLastError());
+    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, codes, codes2, idx, idx2, n, 0, 30,
+                                       stream));
+    CK(cudaMalloc(&tmp, tmp_bytes));
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, codes, codes2, idx, idx2, n, 0, 30,
+                                       stream));
+    k_karras<<<(nn + B - 1) / B, B, 0, stream>>>(codes2, n, s.nodes, leaf_parent);
+    CK(cudaGetLastError());
+    k_refit<<<G, B, 0, stream>>>(lo, hi, idx2, leaf_parent, n, s.box_pad, s.nodes, node_lo,
+                                 node_hi, visits);
+    CK(cudaGetLastError());
+    k_depth<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, dmax);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&depth, dmax, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  }
+  k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris, s.nrm);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(stream));
+  s.num_nodes = nn;
+  s.max_depth = depth;
+  if (depth > 62) {
+    snprintf(err, errlen, "LBVH depth %d exceeds the 62 levels of the traversal trail", depth);
+    rc = cudaErrorInvalidValue;
+  }
+done:
+  cudaFree(lo);
+  cudaFree(hi);
+  cudaFree(bounds);
+  cudaFree(codes);
+  cudaFree(codes2);
+  cudaFree(idx);
+  cudaFree(idx2);
+  cudaFree(leaf_parent);
+  cudaFree(node_lo);
+  cudaFree(node_hi);
+  cudaFree(visits);
+  cudaFree(dmax);
+  cudaFree(tmp);
+  return rc;
+}
+
+}  // namespace ear

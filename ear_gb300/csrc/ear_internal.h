@@ -1,0 +1,123 @@
+// ear_internal.h -- device-side data layout shared by the LBVH builder, the
+// trace kernels and the C-ABI implementation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ear_math.cuh"
+
+namespace ear {
+
+// BVH2 node, 64 bytes, both child boxes stored in the parent so one visit
+// tests two boxes with four 16-byte loads.  Child index >= 0 is an internal
+// node; < 0 is a leaf: ~child = first triangle (leaf order) | (count-1) << 27.
+struct __align__(16) Node {
+  float4 a;  // c0.lo.x c0.hi.x c0.lo.y c0.hi.y
+  float4 b;  // c0.lo.z c0.hi.z c1.lo.x c1.hi.x
+  float4 c;  // c1.lo.y c1.hi.y c1.lo.z c1.hi.z
+  int4 d;    // child0 child1 parent depth
+};
+
+constexpr int kLeafCountShift = 27;
+constexpr int kLeafStartMask = (1 << kLeafCountShift) - 1;
+
+// Triangles in leaf order, 48 bytes each for the Moller-Trumbore test:
+//   tri[3i+0] = (v0.xyz, original index as int bits)
+//   tri[3i+1] = (e1 = v1 - v0, 0), tri[3i+2] = (e2 = v2 - v0, 0)
+// and 16 bytes of shading data: nrm[i] = (unit normal, material id bits).
+
+struct DeviceScene {
+  int64_t num_tris = 0;
+  int64_t num_nodes = 0;
+  int max_depth = 0;
+  float box_pad = 0.0f;
+  Node* nodes = nullptr;
+  float4* tris = nullptr;
+  float4* nrm = nullptr;
+  // inputs kept on the device in file order
+  float* vertices = nullptr;  // [n][9]
+  int32_t* mat_ids = nullptr;
+};
+
+constexpr int kMaxRecorders = 32;
+constexpr int kMaxTracks = 2 * kMaxRecorders;
+
+struct DevMaterial {
+  float survival[3];
+  float p_reflect[3];
+  float spec[3];
+  uint32_t always_reflect;
+};
+
+struct DevRecorder {
+  float loc[3];
+  float right[3];
+  float head_size;
+  float habs[3];
+  int channels;
+  int track0;
+};
+
+// Everything one trace launch needs, passed by value (param space).
+struct TraceArgs {
+  const Node* nodes;
+  const float4* tris;
+  const float4* nrm;
+  int num_tris;
+  int num_nodes;
+  const DevMaterial* mats;
+  int num_mats;
+  const DevRecorder* recs;  // uniform index in the recorder loop
+  int num_recs;
+  // source
+  float src[3];
+  const float4* emitter;  // [n][4]: (a, area) (b, 0) (c, 0) (normal, 0)
+  int num_emitter;
+  float emitter_total_area;
+  // rng
+  uint32_t k0, k1, context;
+  // work: item w -> band = bands[w / num_rays], ray = w % num_rays
+  uint64_t num_rays;
+  uint64_t num_items;
+  int bands[3];
+  int max_bounces;
+  double cutoff;
+  float air[3];  // 1 - air absorption, per band
+  float box_pad;
+  // histogram [track][band][stride]
+  float* hist;
+  int stride;
+  int num_bins;
+  int num_tracks;
+  int2* first_last;  // [track][band]
+  unsigned long long* counters;  // [0] work, [1] segments, [2] shadow, [3] contrib, [4] overflow
+  int* error_flag;
+  int traverse_budget;
+  // debug
+  int dbg_band;
+  int dbg_max_record;
+  int64_t dbg_rays;
+  int32_t* dbg_hit;
+  uint8_t* dbg_bt;
+  uint32_t* dbg_vis;
+};
+
+enum Counter { kWork = 0, kSegments = 1, kShadow = 2, kContrib = 3, kOverflow = 4, kNumCounters = 8 };
+enum ErrorBits { kErrBudget = 1 };
+
+// LBVH build (bvh_build.cu).  Returns a cudaError_t; `err` receives a
+// message on failure.
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char* err, size_t errlen);
+
+// Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
+struct TraceOps {
+  cudaError_t (*trace)(const TraceArgs& a, int grid, size_t smem, bool debug, cudaStream_t s);
+  cudaError_t (*direct)(const TraceArgs& a, float dry, cudaStream_t s);
+  cudaError_t (*occupancy)(bool debug, size_t smem, int* blocks_per_sm);
+  int block;
+};
+extern const TraceOps kTraceExact;
+extern const TraceOps kTraceFast;
+
+}  // namespace ear

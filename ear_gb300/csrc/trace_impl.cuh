@@ -1,0 +1,602 @@
+// trace_impl.cuh -- the sm_103a bounce-loop kernel.  Included twice:
+// trace_exact.cu (EAR_NS = exact, --fmad=false: bit-identical to the CPU
+// restatement) and trace_fast.cu (EAR_NS = fast, FMA contraction allowed).
+//
+// Replaces the per-ray loop of Scene::Render (src/Scene.cpp:124-284) and
+// the two brute-force triangle loops it calls (src/Mesh.cpp:33-71).
+//
+// Structure: a persistent kernel; every warp keeps 32 independent rays in
+// flight.  Each loop iteration advances every live lane by one bounce
+// (closest hit, material choice, new direction, R visibility queries and
+// splats).  Lanes whose path ended are refilled from a global work counter
+// with one atomic per warp (ballot + popc + shuffle), so warps stay full
+// while path lengths vary from 1 to max_bounces.  BVH traversal is
+// stackless: a 64-bit trail records, per level of the current root path,
+// whether the far child is still pending; backtracking climbs parent links.
+#pragma once
+
+#ifndef EAR_NS
+#error "EAR_NS must name the instantiation namespace"
+#endif
+
+#include <limits.h>
+
+#include "ear_internal.h"
+
+namespace ear {
+namespace EAR_NS {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTraceBlock = 256;
+constexpr int kInitialFirstSample = 3 * 44100 - 1;  // src/Recorder.cpp:46
+
+struct Ray {
+  float ox, oy, oz;
+  float ix, iy, iz;
+};
+
+__device__ __forceinline__ float safe_inv(float d) {
+  // 1/d with zero components replaced by +-1e-30 so slabs stay finite.
+  const float dd = (d != 0.0f) ? d : copysignf(1e-30f, d);
+  return 1.0f / dd;
+}
+
+__device__ __forceinline__ Ray make_ray(V3 o, V3 d) {
+  Ray r;
+  r.ox = o.x;
+  r.oy = o.y;
+  r.oz = o.z;
+  r.ix = safe_inv(d.x);
+  r.iy = safe_inv(d.y);
+  r.iz = safe_inv(d.z);
+  return r;
+}
+
+// Slab test against [lo, hi] for t in [0, tmax]; conservative only.
+__device__ __forceinline__ bool box_hit(float lx, float hx, float ly, float hy, float lz, float hz,
+                                        const Ray& r, float tmax, float& tnear) {
+  const float tx0 = (lx - r.ox) * r.ix, tx1 = (hx - r.ox) * r.ix;
+  const float ty0 = (ly - r.oy) * r.iy, ty1 = (hy - r.oy) * r.iy;
+  const float tz0 = (lz - r.oz) * r.iz, tz1 = (hz - r.oz) * r.iz;
+  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+  const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+  tnear = tn;
+  return tn <= tf;
+}
+
+// Moller & Trumbore (1997), non-culling branch, same operation order as the
+// CPU restatement of gmtl::intersectDoubleSided (src/Mesh.cpp:40,65).
+__device__ __forceinline__ bool mt_intersect(const float4& A, const float4& B, const float4& C,
+                                             V3 o, V3 d, float& t) {
+  const V3 e1 = mk(B.x, B.y, B.z), e2 = mk(C.x, C.y, C.z);
+  const V3 pvec = cross(d, e2);
+  const float det = dot(e1, pvec);
+  if (det > -1e-6f && det < 1e-6f) return false;
+  const float inv_det = 1.0f / det;
+  const V3 tvec = sub(o, mk(A.x, A.y, A.z));
+  const float u = dot(tvec, pvec) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  const V3 qvec = cross(tvec, e1);
+  const float v = dot(d, qvec) * inv_det;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  t = dot(e2, qvec) * inv_det;
+  return true;
+}
+
+struct Hit {
+  float t;
+  int pos;   // leaf-order position, -1 = none
+  int orig;  // original (file-order) index
+};
+
+// Returns true (ANY) when the segment is blocked.
+template <bool ANY>
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int code, V3 o, V3 d,
+                                          Hit& h) {
+  const int start = (~code) & kLeafStartMask;
+  const int cnt = ((~code) >> kLeafCountShift) + 1;
+  for (int k = 0; k < cnt; ++k) {
+    const float4* T = tris + 3 * (start + k);
+    const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
+    float t;
+    if (mt_intersect(A, B, C, o, d, t)) {
+      if (ANY) {
+        // Mesh::LineIntersection: 1e-5 < t < 1 (src/Mesh.cpp:65)
+        if (t > 1e-5f && t < 1.0f) return true;
+      } else {
+        // Mesh::RayIntersection: t > 0.001, strict t < d, lowest index on
+        // ties (src/Mesh.cpp:40) == lexicographic min of (t, index).
+        const int orig = __float_as_int(A.w);
+        if (t > 0.001f && (t < h.t || (t == h.t && orig < h.orig))) {
+          h.t = t;
+          h.pos = start + k;
+          h.orig = orig;
+        }
+      }
+    }
+  }
+  return false;
+}
+
+// Stackless traversal.  Closest hit (ANY = false): h receives the hit.
+// Any hit (ANY = true): returns true when blocked.  `slack` widens the
+// t-range culling so rounding in the slab test never removes a candidate.
+template <bool ANY>
+__device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float slack, Hit& h,
+                         bool& budget_hit) {
+  h.t = tlimit;
+  h.pos = -1;
+  h.orig = INT_MAX;
+  if (a.num_tris == 0) return false;
+  const Ray r = make_ray(o, d);
+  int cur = 0;
+  unsigned long long trail = 1ull;
+  int iters = 0;
+  const Node* __restrict__ nodes = a.nodes;
+  for (;;) {
+    if (++iters > a.traverse_budget) {
+      budget_hit = true;
+      return false;
+    }
+    const Node* nd = nodes + cur;
+    const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
+    const int4 ch = __ldg(&nd->d);
+    const float lim = ANY ? tlimit + slack : h.t + (h.t * 2.44140625e-4f + slack);
+    float t0, t1;
+    bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
+    bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
+    if (h0 && ch.x < 0) {
+      if (leaf_test<ANY>(a.tris, ch.x, o, d, h)) return true;
+      h0 = false;
+    }
+    if (h1 && ch.y < 0) {
+      if (leaf_test<ANY>(a.tris, ch.y, o, d, h)) return true;
+      h1 = false;
+    }
+    if (h0 || h1) {
+      if (h0 && h1) {
+        trail = (trail << 1) | 1ull;
+        cur = (t0 <= t1) ? ch.x : ch.y;
+      } else {
+        trail <<= 1;
+        cur = h0 ? ch.x : ch.y;
+      }
+      continue;
+    }
+    // backtrack to the deepest level whose far child is pending
+    for (;;) {
+      if (trail == 1ull) return false;
+      if (trail & 1ull) {
+        trail ^= 1ull;
+        const int par = __ldg(&nodes[cur].d.z);
+        const int4 pc = __ldg(&nodes[par].d);
+        cur = (pc.x == cur) ? pc.y : pc.x;
+        break;
+      }
+      trail >>= 1;
+      cur = __ldg(&nodes[cur].d.z);
+      if (++iters > a.traverse_budget) {
+        budget_hit = true;
+        return false;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- sampling
+// Sample_Sphere / Sample_Hemi (src/Distributions.h:48-67): one Philox
+// block per try; try 0's block is passed in (its 4th word also drives the
+// material choice).
+__device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t band, uint64_t ray,
+                                           uint32_t bounce, bool hemi, V3 n, U4 b, V3& out) {
+  for (int tr = 0; tr < kMaxTries; ++tr) {
+    if (tr) b = rng_block(a.k0, a.k1, a.context, band, ray, 0, bounce, (uint32_t)tr);
+    const float f1 = uniform24(b.x) * 2.0f - 1.0f;
+    const float f2 = uniform24(b.y) * 2.0f - 1.0f;
+    const float f3 = uniform24(b.z) * 2.0f - 1.0f;
+    const float l = (f1 * f1 + f2 * f2) + f3 * f3;
+    if (l < 0.001f || l > 1.0f) continue;
+    const float sl = f_sqrt(l);
+    const V3 v = mk(f1 / sl, f2 / sl, f3 / sl);
+    if (hemi && dot(n, v) < 0.0f) continue;
+    out = v;
+    return true;
+  }
+  out = mk(0.0f, 0.0f, 1.0f);
+  return false;
+}
+
+// ---------------------------------------------------------------- splats
+struct Track {
+  float* row;
+  int* first;  // shared-memory bookkeeping of this (track, band)
+  int* last;
+};
+
+// Adds the triangular splat v_0 = ampl, v_{i+1} = v_i - step at positions
+// s .. s+w-1 (src/MonoRecorder.cpp:90-93), skipping negative positions
+// (src/StereoRecorder.cpp:93) and positions beyond the window.  Groups of
+// four aligned bins go out as one 16-byte vector reduction.
+__device__ __forceinline__ void splat(const Track& tr, int nb, long long s, int w, float ampl,
+                                      float step) {
+  const long long lastpos = s + w - 1;
+  if (lastpos < 0) return;
+  const long long firstpos = s < 0 ? 0 : s;
+  atomicMin(tr.first, (int)(firstpos < nb ? firstpos : nb));
+  atomicMax(tr.last, (int)(lastpos < nb ? lastpos : nb));
+  if (firstpos >= nb) return;
+  float v = ampl;
+  float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int grp = -1;
+  for (int i = 0; i < w; ++i) {
+    const long long pos = s + i;
+    if (pos >= 0 && pos < nb) {
+      const int g = (int)(pos >> 2);
+      if (g != grp) {
+        if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(tr.row + 4 * grp), acc);
+        acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        grp = g;
+      }
+      const int c = (int)(pos & 3);
+      acc.x = c == 0 ? v : acc.x;
+      acc.y = c == 1 ? v : acc.y;
+      acc.z = c == 2 ? v : acc.z;
+      acc.w = c == 3 ? v : acc.w;
+    }
+    v -= step;
+  }
+  if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(tr.row + 4 * grp), acc);
+}
+
+// (int)(t * 44100.0) in double as the reference does; values that do not
+// fit an int are treated as beyond the window.
+__device__ __forceinline__ long long sample_index(float t) {
+  const double ts = (double)t * 44100.0;
+  if (!(ts < 2147483647.0) || !(ts > -2147483648.0)) return (long long)1 << 40;
+  return (long long)(int)ts;
+}
+
+__device__ __forceinline__ Track track_of(const TraceArgs& a, int* s_first, int* s_last,
+                                          int track, int band) {
+  Track tr;
+  tr.row = a.hist + ((size_t)track * 3 + band) * (size_t)a.stride;
+  tr.first = s_first + track * 3 + band;
+  tr.last = s_last + track * 3 + band;
+  return tr;
+}
+
+// MonoRecorder::Record / StereoRecorder::Record (src/MonoRecorder.cpp:83-97,
+// src/StereoRecorder.cpp:97-130).
+__device__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir, float amp,
+                       float t, float dist, int* s_first, int* s_last) {
+  const float width = f_sqrt(dist);
+  const int w = (int)f_ceil(width);
+  if (R.channels == 2) {
+    const float dt = dot(dir, mk(R.right[0], R.right[1], R.right[2]));
+    const float time_difference = R.head_size / 343.0f;
+    const long long s_right = sample_index(t - (dt * time_difference));
+    const long long s_left = sample_index(t + (dt * time_difference));
+    const float ampl = 2.0f * amp / width;
+    float al = ampl, ar = ampl;
+    const float factor = powf_portable(R.habs[band], f_abs(dt) * R.head_size);
+    if (dt < 0) {
+      ar *= factor * factor;
+    } else {
+      al *= factor * factor;
+    }
+    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s_left, w, al, al / (float)w);
+    splat(track_of(a, s_first, s_last, R.track0 + 1, band), a.num_bins, s_right, w, ar,
+          ar / (float)w);
+  } else {
+    const long long s = sample_index(t);
+    const float ampl = 2.0f * amp / width;
+    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s, w, ampl, ampl / (float)w);
+  }
+}
+
+// --------------------------------------------------------------- paths
+struct PathState {
+  V3 o, d, prev;
+  float I, L;
+  int k;
+  int band;
+  uint64_t ray;
+};
+
+struct LaneCounters {
+  uint32_t segments, shadow, contrib, overflow;
+};
+
+// Visibility + contribution for every recorder at the current vertex
+// (src/Scene.cpp:185-270).  bt: 0 REFLECT, 1 REFRACT.
+__device__ __forceinline__ uint32_t connect_recorders(const TraceArgs& a, const PathState& st,
+                                                      V3 n, int bt, float spec_coef, float before,
+                                                      LaneCounters& c, bool& budget_hit,
+                                                      int* s_first, int* s_last) {
+  uint32_t vis = 0;
+  const int k = st.k;
+  for (int ri = 0; ri < a.num_recs; ++ri) {
+    const DevRecorder& R = a.recs[ri];
+    const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
+    c.shadow++;
+    const float len = length(sdir);
+    Hit hh;
+    const float slack = 2.44140625e-4f + a.box_pad / len;
+    if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, budget_hit)) continue;
+    vis |= 1u << (ri & 31);
+    const V3 lsdir = normalized(sdir);
+    const float dt = k ? dot(lsdir, n) : 1.0f;
+    if (!(dt > 0)) continue;
+    float I = before;
+    if (k) {
+      float factor;
+      if (bt == 0) {
+        const V3 refl_vector = reflect(st.prev, n);
+        const float diff_factor = -dot(n, st.prev);
+        const float rv = dot(refl_vector, lsdir);
+        const float spec_factor = (0.0f < rv) ? rv : 0.0f;
+        factor = spec_coef * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+                 (1.0f - spec_coef) * diff_factor;
+      } else {
+        const float diff_factor = dot(n, st.prev);
+        const float rv = dot(st.prev, lsdir);
+        const float spec_factor = (0.0f < rv) ? rv : 0.0f;
+        factor = spec_coef * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+                 (1.0f - spec_coef) * diff_factor;
+      }
+      I *= factor;
+    }
+    I *= powf_portable(a.air[st.band], len);
+    I *= inv_hemi_2(len);
+    if (!invalid_float(I)) {
+      if (k & 1) I *= -1.0f;
+      c.contrib++;
+      const float total = st.L + len;
+      record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last);
+    }
+  }
+  return vis;
+}
+
+template <bool DEBUG>
+__device__ __forceinline__ void debug_put(const TraceArgs& a, const PathState& st, int k, int hit,
+                                          int bt, uint32_t vis, int what) {
+  if (!DEBUG) return;
+  if (st.band != a.dbg_band || (int64_t)st.ray >= a.dbg_rays || k < 1 || k > a.dbg_max_record)
+    return;
+  const size_t i = (size_t)st.ray * a.dbg_max_record + (k - 1);
+  if (what == 0) a.dbg_hit[i] = hit;
+  if (what == 1) a.dbg_bt[i] = (uint8_t)bt;
+  if (what == 2) a.dbg_vis[i] = vis;
+}
+
+// Bounce 0: AbstractSoundFile::SoundRay (src/SoundFile.cpp:215-228) and,
+// for area emitters, the bounce-0 connections (src/Scene.cpp:185).
+// Returns whether the path continues.
+__device__ bool emit(const TraceArgs& a, PathState& st, LaneCounters& c, bool& budget_hit,
+                     int* s_first, int* s_last) {
+  st.I = 1.0f;
+  st.L = 0.0f;
+  st.k = 0;
+  const uint32_t band = (uint32_t)st.band;
+  const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, 0, 0);
+  if (a.num_emitter > 0) {
+    // Mesh::SamplePoint (src/Mesh.cpp:143-154): linear walk of the area CDF
+    const U4 e = rng_block(a.k0, a.k1, a.context, band, st.ray, 1, 0, 0);
+    float x = uniform24(e.x) * a.emitter_total_area;
+    V3 p = mk(0, 0, 0), en = mk(0, 0, 0);
+    for (int i = 0; i < a.num_emitter; ++i) {
+      const float4 A = __ldg(a.emitter + 4 * i);
+      x -= A.w;
+      if (x < 0) {
+        const float4 B = __ldg(a.emitter + 4 * i + 1), C = __ldg(a.emitter + 4 * i + 2),
+                     N = __ldg(a.emitter + 4 * i + 3);
+        const float r1 = uniform24(e.y), r2 = uniform24(e.z);
+        const float sr1 = f_sqrt(r1);
+        const float wa = 1.0f - sr1, wb = sr1 * (1.0f - r2), wc = sr1 * r2;
+        p = mk((wa * A.x + wb * B.x) + wc * C.x, (wa * A.y + wb * B.y) + wc * C.y,
+               (wa * A.z + wb * B.z) + wc * C.z);
+        en = mk(N.x, N.y, N.z);
+        break;
+      }
+    }
+    st.o = p;
+    if (!sample_dir(a, band, st.ray, 0, true, en, b0, st.d)) c.overflow++;
+    // bounce-0 connections of a mesh source, intensity 1
+    connect_recorders(a, st, mk(0, 0, 0), 0, 0.0f, st.I, c, budget_hit, s_first, s_last);
+  } else {
+    st.o = mk(a.src[0], a.src[1], a.src[2]);
+    if (!sample_dir(a, band, st.ray, 0, false, mk(0, 0, 0), b0, st.d)) c.overflow++;
+  }
+  if ((double)st.I < a.cutoff) return false;
+  st.prev = normalized(st.d);
+  return a.max_bounces > 0;
+}
+
+// One reflection k = st.k + 1 (src/Scene.cpp:150-280).
+template <bool DEBUG>
+__device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats, PathState& st,
+                       LaneCounters& c, bool& budget_hit, int* s_first, int* s_last) {
+  const int k = st.k + 1;
+  const uint32_t band = (uint32_t)st.band;
+  c.segments++;
+  Hit h;
+  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, budget_hit);
+  debug_put<DEBUG>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
+  if (h.pos < 0) return false;
+  const float4 nm = __ldg(a.nrm + h.pos);
+  const float t = h.t;
+  const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
+  const V3 N = mk(nm.x, nm.y, nm.z);
+  V3 n = (dot(N, st.d) > 0.0f) ? neg(N) : N;
+  const DevMaterial& M = mats[__float_as_int(nm.w)];
+  // Material::Bounce (src/Material.cpp:76-83)
+  const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, (uint32_t)k, 0);
+  int bt = 0;
+  if (!((M.always_reflect >> band) & 1u)) bt = (uniform24(b0.w) <= M.p_reflect[band]) ? 0 : 1;
+  debug_put<DEBUG>(a, st, k, 0, bt, 0, 1);
+  const float spec = M.spec[band];
+  V3 base;
+  if (bt == 1) {
+    n = neg(n);
+    base = st.d;
+  } else {
+    base = reflect(st.d, n);
+  }
+  V3 v;
+  if (!sample_dir(a, band, st.ray, (uint32_t)k, true, n, b0, v)) c.overflow++;
+  const float om = 1.0f - spec;
+  v = normalized(mk(v.x * om + base.x * spec, v.y * om + base.y * spec, v.z * om + base.z * spec));
+  const float l = length(sub(p, st.o));
+  st.I *= powf_portable(a.air[band], l);
+  st.L += l;
+  st.o = p;
+  st.d = v;
+  st.k = k;
+  st.I *= M.survival[band];
+  const float before = st.I;
+  if (invalid_float(st.I)) return false;
+  const uint32_t vis =
+      connect_recorders(a, st, n, bt, spec, before, c, budget_hit, s_first, s_last);
+  debug_put<DEBUG>(a, st, k, 0, 0, vis, 2);
+  if ((double)st.I < a.cutoff) return false;
+  st.prev = normalized(st.d);
+  return k < a.max_bounces;
+}
+
+template <bool DEBUG>
+__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DevMaterial* s_mats = reinterpret_cast<DevMaterial*>(smem_raw);
+  int* s_first = reinterpret_cast<int*>(smem_raw + sizeof(DevMaterial) * a.num_mats);
+  int* s_last = s_first + a.num_tracks * 3;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.mats);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_mats);
+    const int words = (int)(sizeof(DevMaterial) / 4) * a.num_mats;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+    for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
+      s_first[i] = kInitialFirstSample;
+      s_last[i] = 0;
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  LaneCounters c = {0, 0, 0, 0};
+  bool budget_hit = false;
+  bool alive = false, exhausted = false;
+  PathState st;
+  st.k = 0;
+  st.band = 0;
+  st.ray = 0;
+  for (;;) {
+    const unsigned need = __ballot_sync(kFull, !alive && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(a.counters + kWork, (unsigned long long)__popc(need));
+      base = __shfl_sync(kFull, base, leader);
+      if (!alive && !exhausted) {
+        const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+        if (w < a.num_items) {
+          const uint64_t bi = w / a.num_rays;
+          st.band = a.bands[bi];
+          st.ray = w - bi * a.num_rays;
+          alive = emit(a, st, c, budget_hit, s_first, s_last);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(kFull, exhausted)) break;
+    if (alive) alive = bounce<DEBUG>(a, s_mats, st, c, budget_hit, s_first, s_last);
+  }
+  // flush statistics: one atomic per warp and counter
+  {
+    const uint32_t seg = __reduce_add_sync(kFull, c.segments);
+    const uint32_t sh = __reduce_add_sync(kFull, c.shadow);
+    const uint32_t co = __reduce_add_sync(kFull, c.contrib);
+    const uint32_t ov = __reduce_add_sync(kFull, c.overflow);
+    if (lane == 0) {
+      atomicAdd(a.counters + kSegments, (unsigned long long)seg);
+      atomicAdd(a.counters + kShadow, (unsigned long long)sh);
+      atomicAdd(a.counters + kContrib, (unsigned long long)co);
+      if (ov) atomicAdd(a.counters + kOverflow, (unsigned long long)ov);
+    }
+    if (__any_sync(kFull, budget_hit) && lane == 0) atomicOr(a.error_flag, kErrBudget);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
+    if (s_last[i] > 0) atomicMax(&a.first_last[i].y, s_last[i]);
+    if (s_first[i] < kInitialFirstSample) atomicMin(&a.first_last[i].x, s_first[i]);
+  }
+}
+
+// End of Scene::Render (src/Scene.cpp:286-316), part 2: the direct-sound
+// lobe, one thread per (recorder, band).  Runs between the two scaling
+// passes; writes go straight to the rows with first/last in global memory.
+__global__ void direct_kernel(const TraceArgs a, float dry) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.num_recs * 3) return;
+  const int ri = i / 3, band = i % 3;
+  bool on = false;
+  for (int b = 0; b < 3; ++b) on |= (a.bands[b] == band);
+  if (!on) return;
+  const DevRecorder& R = a.recs[ri];
+  const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
+  const V3 src = mk(a.src[0], a.src[1], a.src[2]);
+  const V3 seg = sub(src, loc);
+  bool budget_hit = false;
+  Hit hh;
+  const float seglen = length(seg);
+  const float slack = 2.44140625e-4f + (seglen > 0.0f ? a.box_pad / seglen : 0.0f);
+  if (traverse<true>(a, loc, seg, 1.0f, slack, hh, budget_hit)) return;
+  if (budget_hit) atomicOr(a.error_flag, kErrBudget);
+  const V3 dist = sub(loc, src);
+  const float len = length(dist);
+  const V3 dir = normalized(dist);
+  const float amp = inv_sphere_2(len) * powf_portable(a.air[band], len) * dry;
+  int* fl = reinterpret_cast<int*>(a.first_last);
+  // first/last live interleaved as int2 [track][band] -> use strided views
+  int* s_first = fl;      // element (track*3+band)*2
+  int* s_last = fl + 1;   // element (track*3+band)*2 + 1
+  // record() indexes first/last as base + track*3 + band; build per-call
+  // bases with stride 2 by recording through a local shim.
+  const float width = f_sqrt(len);
+  const int w = (int)f_ceil(width);
+  const float t = len / 343.0f;
+  if (R.channels == 2) {
+    const float dt = dot(dir, mk(R.right[0], R.right[1], R.right[2]));
+    const float time_difference = R.head_size / 343.0f;
+    const long long s_right = sample_index(t - (dt * time_difference));
+    const long long s_left = sample_index(t + (dt * time_difference));
+    const float ampl = 2.0f * amp / width;
+    float al = ampl, ar = ampl;
+    const float factor = powf_portable(R.habs[band], f_abs(dt) * R.head_size);
+    if (dt < 0) {
+      ar *= factor * factor;
+    } else {
+      al *= factor * factor;
+    }
+    Track tl, trr;
+    tl.row = a.hist + ((size_t)R.track0 * 3 + band) * (size_t)a.stride;
+    tl.first = s_first + 2 * (R.track0 * 3 + band);
+    tl.last = s_last + 2 * (R.track0 * 3 + band);
+    trr.row = a.hist + ((size_t)(R.track0 + 1) * 3 + band) * (size_t)a.stride;
+    trr.first = s_first + 2 * ((R.track0 + 1) * 3 + band);
+    trr.last = s_last + 2 * ((R.track0 + 1) * 3 + band);
+    splat(tl, a.num_bins, s_left, w, al, al / (float)w);
+    splat(trr, a.num_bins, s_right, w, ar, ar / (float)w);
+  } else {
+    const long long s = sample_index(t);
+    const float ampl = 2.0f * amp / width;
+    Track tm;
+    tm.row = a.hist + ((size_t)R.track0 * 3 + band) * (size_t)a.stride;
+    tm.first = s_first + 2 * (R.track0 * 3 + band);
+    tm.last = s_last + 2 * (R.track0 * 3 + band);
+    splat(tm, a.num_bins, s, w, ampl, ampl / (float)w);
+  }
+}
+
+}  // namespace EAR_NS
+}  // namespace ear

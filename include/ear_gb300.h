@@ -1,0 +1,238 @@
+/*
+ * ear_gb300.h -- C ABI of the GB300 (sm_103a) acoustic ray-tracing core.
+ *
+ * This is the drop-in boundary for E.A.R's ray-tracing path.  The reference
+ * (aothms/ear) has no plugin or FFI layer; its seam is the C++ method
+ *
+ *   void Scene::Render(int band, int sound, float absorbtion_factor,
+ *                      int num_samples, float dry,
+ *                      const std::vector<Recorder*>& rec, int keyframeID)
+ *                                                   (src/Scene.h:77)
+ *
+ * called once per (source x keyframe x band) context by
+ * SceneContext::operator() (src/SceneContext.h:46-48) from the thread groups
+ * in Render() (src/EAR.cpp:193-207).  ear_render() below replaces that call
+ * for all bands of one (source, keyframe) context at once; the inner seams
+ * Mesh::RayIntersection / Mesh::LineIntersection (src/Mesh.h:54-55) are
+ * exposed for parity testing through ear_trace_debug().
+ *
+ * Conventions
+ *  - Plain C types only; every function returns an ear_status.  On failure
+ *    ear_last_error() returns a thread-local message.
+ *  - Bands are 0 = low, 1 = mid, 2 = high, as in the reference.
+ *  - Histogram ("track") layout: float[num_tracks][3][num_bins], tracks in
+ *    recorder order (a mono recorder owns 1 track, a stereo recorder 2:
+ *    left then right, src/StereoRecorder.cpp:124-129).  Samples are at
+ *    44.1 kHz (src/Recorder.h:35).
+ *  - Output pointers are host memory unless ear_histograms.on_device is set.
+ *  - A scene handle is not re-entrant; distinct handles may be used from
+ *    distinct host threads.  All work is issued on ear_render_params.stream
+ *    (NULL = the legacy default stream) and the call returns after it is
+ *    complete.
+ */
+#ifndef EAR_GB300_H
+#define EAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EAR_ABI_VERSION 1
+#define EAR_NUM_BANDS 3
+#define EAR_SAMPLE_RATE 44100
+/* Loop bound of Scene::Render: 1000 iterations = emission + 999 reflections
+ * (src/Scene.cpp:143). */
+#define EAR_REFERENCE_MAX_BOUNCES 999
+/* Path cut-off of Scene::Render (src/Scene.cpp:275). */
+#define EAR_REFERENCE_CUTOFF 1e-8
+
+typedef enum ear_status {
+  EAR_OK = 0,
+  EAR_ERR_INVALID_ARG = 1,   /* bad pointer, size or value */
+  EAR_ERR_OUT_OF_MEMORY = 2, /* device or host allocation failed */
+  EAR_ERR_CUDA = 3,          /* a CUDA runtime call failed */
+  EAR_ERR_DEVICE_BUDGET = 4, /* a device loop hit its iteration budget */
+  EAR_ERR_STATE = 5,         /* e.g. ear_render before ear_scene_build_bvh */
+  EAR_ERR_UNSUPPORTED = 6
+} ear_status;
+
+/* Render flags. */
+#define EAR_FLAG_EXACT 0x1u      /* use the kernels compiled with --fmad=false:
+                                    bit-exact with the CPU oracle */
+#define EAR_FLAG_RAW 0x2u        /* return raw splat sums: no 1/N scaling, no
+                                    direct sound, no gain (for split renders) */
+#define EAR_FLAG_NO_DIRECT 0x4u  /* skip the direct-sound lobe only */
+
+typedef struct ear_scene ear_scene; /* opaque: device geometry + LBVH */
+
+/* One MAT block (src/Material.cpp:26-72).  Values are per band.  A block
+ * without a refraction triplet is opaque (has_refraction = 0), one without
+ * a specularity triplet has specularity 0 (the std::map default read at
+ * src/Scene.cpp:163). */
+typedef struct ear_material {
+  float reflection[3];
+  float refraction[3];
+  float specularity[3];
+  int32_t has_refraction;
+  int32_t has_specularity;
+} ear_material;
+
+/* All MESH blocks merged in file order, as Scene::addMesh / Mesh::Combine
+ * do (src/Scene.cpp:103-106, src/Mesh.cpp:116-123): triangle i of this
+ * array is triangle i of the reference's meshes[0]->tris. */
+typedef struct ear_scene_desc {
+  int64_t num_triangles;
+  const float* vertices;       /* host, num_triangles * 9 floats (v0 v1 v2) */
+  const int32_t* material_ids; /* host, num_triangles indices into materials */
+  int32_t num_materials;
+  const ear_material* materials;
+  int32_t device;              /* CUDA device ordinal */
+} ear_scene_desc;
+
+typedef struct ear_bvh_opts {
+  /* Padding added to every triangle's bounding box, in scene units.  Values
+     < 0 select the default (2^-14 of the largest absolute coordinate plus
+     1e-6).  Padding only makes the culling conservative; it never changes
+     which triangle is reported. */
+  float box_pad;
+  int32_t reserved[7];
+} ear_bvh_opts;
+
+/* OUT1 (mono, src/MonoRecorder.cpp:38-59) or OUT2 (stereo,
+ * src/StereoRecorder.cpp:33-67) block, evaluated at the keyframe being
+ * rendered (Animated<T>::Evaluate, src/Animated.h:89-91). */
+typedef struct ear_recorder {
+  int32_t channels;           /* 1 = mono, 2 = stereo */
+  float location[3];
+  float right_ear[3];         /* stereo only */
+  float head_size;            /* stereo only */
+  float head_absorption[3];   /* stereo only; the value written in the file,
+                                 transformed as src/StereoRecorder.cpp:55-57 */
+} ear_recorder;
+
+/* SSRC / 3SRC block (src/SoundFile.cpp:33-70, 84-117) at one keyframe. */
+typedef struct ear_source {
+  float location[3];               /* point source */
+  float gain;                      /* squared into the response, :313-314 */
+  int64_t num_emitter_triangles;   /* > 0: area (mesh) emitter */
+  const float* emitter_vertices;   /* host, num_emitter_triangles * 9 */
+} ear_source;
+
+typedef struct ear_render_params {
+  uint64_t seed;           /* Philox-4x32-10 key */
+  uint32_t context;        /* folded into every RNG counter: distinct
+                              (source, keyframe) contexts use distinct ids */
+  uint32_t bands_mask;     /* bit b set: trace band b */
+  uint64_t num_rays;       /* rays per band (Scene::Render num_samples) */
+  int32_t max_bounces;     /* maximum reflections per ray; the reference's
+                              loop allows EAR_REFERENCE_MAX_BOUNCES */
+  int32_t num_bins;        /* histogram length in samples */
+  double cutoff;           /* path ends when intensity < cutoff */
+  float air_absorption[3]; /* 'absorption' setting: factor = 1 - a (EAR.cpp:180) */
+  float dry_level;         /* 'drylevel' setting */
+  uint32_t flags;          /* EAR_FLAG_* */
+  int32_t reserved0;
+  void* stream;            /* cudaStream_t, NULL = default stream */
+} ear_render_params;
+
+/* Per-render statistics (counted on the device). */
+typedef struct ear_render_stats {
+  uint64_t rays;           /* primary rays emitted */
+  uint64_t segments;       /* closest-hit queries for bounces k >= 1 */
+  uint64_t shadow_queries; /* any-hit (visibility) queries */
+  uint64_t contributions;  /* valid recorded path contributions */
+  uint64_t sampler_overflows; /* rejection loops that reached their bound */
+  double kernel_ms;        /* device time of the trace kernel(s) */
+} ear_render_stats;
+
+typedef struct ear_histograms {
+  float* data;             /* [num_tracks][3][num_bins] */
+  /* FloatBuffer bookkeeping per [track][band] (src/Recorder.cpp:43-59):
+     first_sample = min(132299, smallest index written) and last_sample =
+     max(0, largest index written) ("real_length"), both clamped to
+     num_bins (num_bins = something was written beyond the window). */
+  int32_t* first_sample;   /* optional, [num_tracks][3] */
+  int32_t* last_sample;    /* optional, [num_tracks][3] */
+  int32_t on_device;       /* data/first/last are device pointers */
+  int32_t reserved0;
+} ear_histograms;
+
+/* ---------------------------------------------------------------- errors */
+const char* ear_last_error(void);
+const char* ear_version(void);
+int32_t ear_abi_version(void);
+
+/* ----------------------------------------------------------------- scene */
+/* Replaces the triangle soup of meshes[0] (src/Mesh.cpp:77-123) and the
+   static material map (src/Mesh.cpp:178).  Uploads geometry to the device. */
+ear_status ear_scene_create(const ear_scene_desc* desc, ear_scene** out);
+/* Builds the LBVH on the device.  New: the reference has no acceleration
+   structure (src/Scene.h:37-41); brute force is in src/Mesh.cpp:33-71. */
+ear_status ear_scene_build_bvh(ear_scene* scene, const ear_bvh_opts* opts);
+/* Node count, depth, padding actually used, device bytes. */
+ear_status ear_scene_info(const ear_scene* scene, int64_t* num_triangles,
+                          int64_t* num_nodes, int32_t* max_depth,
+                          float* box_pad, int64_t* device_bytes);
+void ear_scene_destroy(ear_scene* scene);
+
+/* Number of tracks the recorders produce (1 per mono, 2 per stereo). */
+int32_t ear_num_tracks(const ear_recorder* recorders, int32_t num_recorders);
+
+/* ---------------------------------------------------------------- render */
+/* Replaces Scene::Render (src/Scene.cpp:111-318) for every band in
+   params->bands_mask of one (source, keyframe) context.  Tracks of bands not
+   in the mask are zeroed.  stats may be NULL. */
+ear_status ear_render(ear_scene* scene, const ear_source* source,
+                      const ear_recorder* recorders, int32_t num_recorders,
+                      const ear_render_params* params, ear_histograms* out,
+                      ear_render_stats* stats);
+
+/* Parity probe: traces the same paths as ear_render (same kernel code) for
+   band `band` and records, for ray r < num_rays and reflection k in
+   [1, max_record]: hit_tri[r*max_record + k-1] = original index of the
+   triangle hit (-1 = miss, -2 = path already ended), bounce_type[...] =
+   0 REFLECT / 1 REFRACT (src/Material.cpp:76-83), visible[...] = bit j set
+   when recorder j is connected (src/Scene.cpp:84-96).  Host pointers. */
+ear_status ear_trace_debug(ear_scene* scene, const ear_source* source,
+                           const ear_recorder* recorders,
+                           int32_t num_recorders,
+                           const ear_render_params* params, int32_t band,
+                           int32_t max_record, int32_t* hit_tri,
+                           uint8_t* bounce_type, uint32_t* visible);
+
+/* --------------------------------------- host post-processing (FloatBuffer)
+ * Mirrors of FloatBuffer / RecorderTrack (src/Recorder.cpp:33-118, 303-340)
+ * on one track.  `first`/`last` are the bookkeeping values above; the track
+ * buffer holds `capacity` samples.  Host memory. */
+/* FloatBuffer::Power, src/Recorder.cpp:103-108 */
+ear_status ear_track_power(float* data, int32_t first, int32_t last, float a);
+/* FloatBuffer::Maximum, src/Recorder.cpp:76-83 */
+float ear_track_maximum(const float* data, int32_t first, int32_t last);
+/* FloatBuffer::Multiply, src/Recorder.cpp:85-89 */
+ear_status ear_track_multiply(float* data, int32_t first, int32_t last, float f);
+/* FloatBuffer::getLength(tresh), src/Recorder.cpp:110-118 */
+int32_t ear_track_length(const float* data, int32_t capacity, int32_t first,
+                         int32_t last, float tresh);
+/* RecorderTrack::T60, src/Recorder.cpp:303-340 */
+float ear_track_t60(const float* data, int32_t first, int32_t last);
+
+/* Sabine and Norris-Eyring predictions of src/EAR.cpp:264-284.  The
+   vertices are the merged MESH blocks (block_triangles[i] triangles each, in
+   file order); as in the reference, the volume and area cover every block
+   but the total absorption only the first block, whose MAT is
+   first_block_material (Mesh::Combine does not add it, src/Mesh.cpp:116-123).
+   out[5] = {volume, area, total absorption, sabine, eyring}. */
+ear_status ear_statistical_t60(const float* vertices,
+                               const int64_t* block_triangles,
+                               int32_t num_blocks,
+                               const ear_material* first_block_material,
+                               float air_absorption_mid, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EAR_GB300_H */

@@ -1,0 +1,147 @@
+"""ctypes binding of the CPU restatement (oracle/ear_oracle.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+the CPU-baseline legs of bench.py, as the checker or the timed baseline.
+The product (ear_gb300) never imports this package.  PARITY UNPINNED: see
+the header of ear_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from ear_gb300 import _native as N
+from ear_gb300.scene import make_params, recorders_at
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libear_oracle.so"
+
+
+class OracleOutput(C.Structure):
+    _fields_ = [("hist64", C.c_void_p), ("hist32", C.c_void_p), ("first_sample", C.c_void_p),
+                ("last_sample", C.c_void_p), ("counters", C.c_void_p), ("debug_band", C.c_int32),
+                ("debug_max_record", C.c_int32), ("debug_rays", C.c_int64), ("hit_tri", C.c_void_p),
+                ("bounce_type", C.c_void_p), ("visible", C.c_void_p)]
+
+
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        if not LIB_PATH.exists():
+            from ear_gb300.build import build_oracle
+            build_oracle()
+        L = C.CDLL(str(LIB_PATH))
+        L.oracle_render.restype = C.c_int
+        L.oracle_render.argtypes = [C.POINTER(N.EarSceneDesc), C.POINTER(N.EarSource),
+                                    C.POINTER(N.EarRecorder), C.c_int32,
+                                    C.POINTER(N.EarRenderParams), C.c_int32, C.c_int32,
+                                    C.POINTER(OracleOutput)]
+        L.oracle_last_error.restype = C.c_char_p
+        L.oracle_powf.restype = C.c_float
+        L.oracle_powf.argtypes = [C.c_float, C.c_float]
+        L.oracle_philox.argtypes = [C.c_uint32] * 6 + [C.c_void_p]
+        L.oracle_material.argtypes = [C.POINTER(N.EarMaterial), C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p]
+        L.oracle_closest_hit.argtypes = [C.POINTER(N.EarSceneDesc), C.c_int64, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_segment_blocked.argtypes = [C.POINTER(N.EarSceneDesc), C.c_int64, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]
+        L.oracle_track_power.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_float]
+        L.oracle_track_maximum.restype = C.c_float
+        L.oracle_track_maximum.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.oracle_track_length.restype = C.c_int32
+        L.oracle_track_length.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float]
+        L.oracle_track_t60.restype = C.c_float
+        L.oracle_track_t60.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        _L = L
+    return _L
+
+
+def scene_desc(vertices, material_ids, materials):
+    v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
+    m = np.ascontiguousarray(material_ids, dtype=np.int32).reshape(-1)
+    mats = (N.EarMaterial * max(1, len(materials)))()
+    for i, mm in enumerate(materials):
+        mats[i] = mm.to_c()
+    d = N.EarSceneDesc()
+    d.num_triangles = v.shape[0]
+    d.vertices = v.ctypes.data_as(C.POINTER(C.c_float))
+    d.material_ids = m.ctypes.data_as(C.POINTER(C.c_int32))
+    d.num_materials = len(materials)
+    d.materials = mats
+    return d, (v, m, mats)
+
+
+def render(vertices, material_ids, materials, source, recorders, *, keyframe=-1, threads=1,
+           pow_mode=0, debug_band=-1, debug_rays=0, debug_max_record=0, **kw):
+    """Scene::Render restated on the CPU for every band in kw['bands'].
+    Returns a dict with hist64 (FP64 re-accumulation), hist32 (float
+    accumulation in ray order per thread chunk), first/last sample, the
+    counters and, when requested, the per-bounce debug record."""
+    d, keep = scene_desc(vertices, material_ids, materials)
+    src, _k2 = source.at(keyframe)
+    recs = recorders_at(recorders, keyframe)
+    p = make_params(**kw)
+    tracks = sum(r.tracks for r in recorders)
+    nb = p.num_bins
+    h64 = np.zeros((max(tracks, 1), 3, nb), np.float64)
+    h32 = np.zeros((max(tracks, 1), 3, nb), np.float32)
+    first = np.zeros((max(tracks, 1), 3), np.int32)
+    last = np.zeros((max(tracks, 1), 3), np.int32)
+    cnt = np.zeros(5, np.uint64)
+    o = OracleOutput()
+    o.hist64, o.hist32 = h64.ctypes.data, h32.ctypes.data
+    o.first_sample, o.last_sample, o.counters = first.ctypes.data, last.ctypes.data, cnt.ctypes.data
+    dbg = None
+    if debug_max_record > 0:
+        hit = np.empty((debug_rays, debug_max_record), np.int32)
+        bt = np.empty((debug_rays, debug_max_record), np.uint8)
+        vis = np.empty((debug_rays, debug_max_record), np.uint32)
+        o.debug_band, o.debug_max_record, o.debug_rays = debug_band, debug_max_record, debug_rays
+        o.hit_tri, o.bounce_type, o.visible = hit.ctypes.data, bt.ctypes.data, vis.ctypes.data
+        dbg = (hit, bt, vis)
+    rc = lib().oracle_render(C.byref(d), C.byref(src), recs, len(recorders), C.byref(p),
+                             int(threads), int(pow_mode), C.byref(o))
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+    out = {"hist64": h64[:tracks], "hist32": h32[:tracks], "first_sample": first[:tracks],
+           "last_sample": last[:tracks],
+           "counters": dict(zip(["rays", "segments", "shadow_queries", "contributions",
+                                 "sampler_overflows"], [int(x) for x in cnt]))}
+    if dbg is not None:
+        out["debug"] = dbg
+    return out
+
+
+def powf(x: float, y: float) -> float:
+    return lib().oracle_powf(x, y)
+
+
+def philox(counter, key):
+    out = (C.c_uint32 * 4)()
+    lib().oracle_philox(*[int(c) for c in counter], *[int(k) for k in key], out)
+    return list(out)
+
+
+def closest_hit(vertices, origins, dirs):
+    d, keep = scene_desc(vertices, np.zeros(len(vertices), np.int32), [])
+    o = np.ascontiguousarray(origins, np.float32)
+    r = np.ascontiguousarray(dirs, np.float32)
+    hit = np.empty(len(o), np.int32)
+    t = np.empty(len(o), np.float32)
+    lib().oracle_closest_hit(C.byref(d), len(o), o.ctypes.data, r.ctypes.data, hit.ctypes.data,
+                             t.ctypes.data)
+    return hit, t
+
+
+def segment_blocked(vertices, origins, dirs):
+    d, keep = scene_desc(vertices, np.zeros(len(vertices), np.int32), [])
+    o = np.ascontiguousarray(origins, np.float32)
+    r = np.ascontiguousarray(dirs, np.float32)
+    out = np.empty(len(o), np.uint8)
+    lib().oracle_segment_blocked(C.byref(d), len(o), o.ctypes.data, r.ctypes.data, out.ctypes.data)
+    return out.astype(bool)
