@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark: ray-bounce segments/s of the GB300 ray-tracing core.
+
+A step is one ear_render of the workload: every band of the (source,
+keyframe) context, all rays, all recorders -- one pass of the hot path
+(Scene::Render, src/Scene.cpp:111-318) over its synthetic scene.  The
+default workload is the 20,000-triangle relief hall (stereo recorder, 3 s
+histograms, 200 reflections) at 1e7 rays per band.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the reference algorithm on the CPU
+
+value      segments/s over the K timed steps, scene resident in HBM, device
+           time (CUDA events around each step on its stream; the L2 is
+           flushed with a 512 MB write before every step, outside the step).
+e2e        the same metric through the C ABI from host memory: scene upload
+           from pinned host buffers, LBVH build, render, histograms read back
+           to the host, scene release -- all inside each timed step.
+roofline   algorithmic bytes of the trace kernel (64 B per node visit, 48 B
+           per triangle test, 64 B of path state per segment, 4 B per splat
+           bin; counted on the device) / its CUDA-event time, against the
+           measured HBM copy bandwidth.
+cpu_baseline  the CPU restatement of the reference algorithm (brute-force
+           triangle loops, oracle/), all host threads, on a bounded ray sample.
+
+Multi-GPU (torchrun): rays are independent, so every rank renders its own
+rays (seed + rank) with no collective in the data path ("weak" scaling);
+rank 0 prints the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "relief_hall": "relief_hall",
+    "shoebox": "shoebox",
+    "cathedral": "cathedral",
+}
+
+
+def load_workload(name: str, num_rays: int | None):
+    from ear_gb300 import scenes
+
+    w = getattr(scenes, WORKLOADS[name])()
+    if num_rays:
+        w.render["num_rays"] = int(num_rays)
+    return w
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if _cuda() else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def _cuda():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _cuda() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _cuda() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(w, sample_rays: int, threads: int):
+    """The CPU restatement of the reference path on a bounded ray sample."""
+    import oracle
+
+    kw = dict(w.render)
+    kw["num_rays"] = sample_rays
+    t0 = time.perf_counter()
+    r = oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
+                      threads=threads, **kw)
+    dt = time.perf_counter() - t0
+    seg = r["counters"]["segments"]
+    return {"value": seg / dt, "unit": "segments/s", "cores": threads, "kind": "port",
+            "sample": f"{sample_rays} rays/band x 3 bands of the same workload "
+                      f"({seg} segments, {dt:.1f} s, brute-force triangle loops)",
+            "seconds": dt, "segments": seg}
+
+
+def run_reference(args):
+    rank, world, local = dist_init(args.gpus)
+    if rank != 0:
+        return 0
+    w = load_workload(args.workload, args.rays)
+    threads = os.cpu_count() or 1
+    sample = args.cpu_rays or _default_cpu_rays(args.workload)
+    for _ in range(args.warmup):
+        cpu_baseline(w, max(1, sample // 10), threads)
+    vals, segs, secs = [], 0, 0.0
+    for _ in range(args.steps):
+        b = cpu_baseline(w, sample, threads)
+        vals.append(b["value"])
+        segs += b["segments"]
+        secs += b["seconds"]
+    v = segs / secs
+    line = {
+        "impl": "reference", "metric": "ray-bounce segments/s", "value": v, "unit": "segments/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": _config(w, args, flush="n/a (CPU)"),
+        "cpu_baseline": {"value": v, "unit": "segments/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} rays/band x 3 bands per step of the workload, "
+                                   "brute-force O(T) loops as the reference"},
+        "e2e": {"value": v, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _default_cpu_rays(name):
+    return {"relief_hall": 300, "shoebox": 20000, "cathedral": 4}.get(name, 100)
+
+
+def _config(w, args, flush):
+    return {"workload": w.name, "triangles": w.num_triangles, "materials": len(w.materials),
+            "recorders": len(w.recorders), "tracks": w.num_tracks,
+            "rays_per_band": w.render["num_rays"], "bands": 3,
+            "max_bounces": w.render["max_bounces"], "histogram_bins": w.render["num_bins"],
+            "cutoff": w.render["cutoff"], "parallelism": f"replicas{args.gpus}",
+            "l2": flush}
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    from ear_gb300 import Tracer, _native as N
+    from ear_gb300.scene import make_params, recorders_at
+
+    rank, world, local = dist_init(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = load_workload(args.workload, args.rays)
+    kw = dict(w.render)
+    kw["seed"] = int(kw.get("seed", 0)) + rank
+    exact = args.exact
+    tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad)
+    tracks = w.num_tracks
+    out = torch.zeros((tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return tracer.render(w.source, w.recorders, out=out, exact=exact, **kw)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    kern_ms = 0.0
+    seg = 0
+    agg = {"node_visits": 0, "triangle_tests": 0, "splat_bins": 0, "segments": 0, "rays": 0,
+           "shadow_queries": 0}
+    launches = 0
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        res = step()
+        s1.record(stream)
+        s1.synchronize()
+        total_ms += s0.elapsed_time(s1)
+        kern_ms += res.stats["kernel_ms"]
+        for k in agg:
+            agg[k] += int(res.stats[k])
+        # per step: trace kernel + 2 scale passes + direct-sound kernel + first/last init
+        launches += 5
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    t_max = max_over_ranks(total_ms, world)
+    seg_all = sum_over_ranks(agg["segments"], world)
+    value = seg_all / (t_max / 1000.0)
+
+    # roofline of the trace kernel: algorithmic bytes / kernel time
+    alg_bytes = 64.0 * agg["node_visits"] + 48.0 * agg["triangle_tests"] + 64.0 * agg["segments"] \
+        + 4.0 * agg["splat_bins"]
+    achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else 0.0
+    hbm, src = peaks()
+    per_launch = alg_bytes / args.steps
+
+    # e2e through the C ABI from pinned host memory, every step
+    e2e = None
+    if not args.no_e2e:
+        vp = torch.from_numpy(np.ascontiguousarray(w.vertices)).pin_memory().numpy()
+        mp = torch.from_numpy(np.ascontiguousarray(w.material_ids)).pin_memory().numpy()
+        host_out = torch.empty((tracks, 3, kw["num_bins"]), dtype=torch.float32).pin_memory()
+        e_steps = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e_seg = 0
+        e0.record(stream)
+        for _ in range(e_steps):
+            t2 = Tracer(vp, mp, w.materials, device=local, box_pad=args.box_pad)
+            r2 = t2.render(w.source, w.recorders, out=host_out, exact=exact, **kw)
+            t2.close()
+            e_seg += int(r2.stats["segments"])
+        e1.record(stream)
+        e1.synchronize()
+        e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+        e_seg_all = sum_over_ranks(e_seg, world)
+        e2e = {"value": e_seg_all / (e_ms / 1000.0), "unit": "segments/s",
+               "h2d_bytes_per_step": int(w.vertices.nbytes + w.material_ids.nbytes),
+               "d2h_bytes_per_step": int(host_out.numel() * 4),
+               "steps": e_steps, "ms_per_step": e_ms / e_steps,
+               "path": "ear_scene_create (pinned host) + ear_scene_build_bvh + ear_render "
+                       "(histograms to pinned host) + ear_scene_destroy"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(w, args.cpu_rays or _default_cpu_rays(args.workload), os.cpu_count() or 1)
+        cpu.pop("seconds", None)
+        cpu.pop("segments", None)
+
+    if rank == 0:
+        cfg = _config(w, args, flush="flushed before every step (512 MB write)")
+        cfg["mode"] = "exact (--fmad=false)" if exact else "fast"
+        cfg["rays_per_s"] = agg["rays"] / (total_ms / 1000.0) * world
+        line = {
+            "metric": "ray-bounce segments/s", "value": value, "unit": "segments/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": cfg,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "peak_source": src, "kernel": "trace_kernel<false>",
+                         "algorithmic_bytes_per_launch": per_launch,
+                         "kernel_ms_per_launch": kern_ms / args.steps},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    tracer.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="relief_hall", choices=sorted(WORKLOADS))
+    ap.add_argument("--rays", type=int, default=None, help="rays per band (default: the config's)")
+    ap.add_argument("--cpu-rays", type=int, default=None)
+    ap.add_argument("--exact", action="store_true")
+    ap.add_argument("--box-pad", type=float, default=-1.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

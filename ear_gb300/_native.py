@@ -66,7 +66,8 @@ class EarRenderParams(C.Structure):
 class EarRenderStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("segments", C.c_uint64), ("shadow_queries", C.c_uint64),
                 ("contributions", C.c_uint64), ("sampler_overflows", C.c_uint64),
-                ("kernel_ms", C.c_double)]
+                ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64),
+                ("splat_bins", C.c_uint64), ("kernel_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -437,6 +437,9 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
     stats->shadow_queries = cnt[kShadow];
     stats->contributions = cnt[kContrib];
     stats->sampler_overflows = cnt[kOverflow];
+    stats->node_visits = cnt[kNodeVisits];
+    stats->triangle_tests = cnt[kTriTests];
+    stats->splat_bins = cnt[kSplatBins];
     stats->kernel_ms = ms;
   }
   return EAR_OK;

@@ -103,7 +103,17 @@ struct TraceArgs {
   uint32_t* dbg_vis;
 };
 
-enum Counter { kWork = 0, kSegments = 1, kShadow = 2, kContrib = 3, kOverflow = 4, kNumCounters = 8 };
+enum Counter {
+  kWork = 0,
+  kSegments = 1,
+  kShadow = 2,
+  kContrib = 3,
+  kOverflow = 4,
+  kNodeVisits = 5,  // internal-node visits (64 B each)
+  kTriTests = 6,    // Moller-Trumbore tests (48 B each)
+  kSplatBins = 7,   // histogram bins written
+  kNumCounters = 8
+};
 enum ErrorBits { kErrBudget = 1 };
 
 // LBVH build (bvh_build.cu).  Returns a cudaError_t; `err` receives a

@@ -89,12 +89,17 @@ struct Hit {
   int orig;  // original (file-order) index
 };
 
+struct LaneCounters {
+  uint32_t segments, shadow, contrib, overflow, nodes, tris, bins;
+};
+
 // Returns true (ANY) when the segment is blocked.
 template <bool ANY>
 __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int code, V3 o, V3 d,
-                                          Hit& h) {
+                                          Hit& h, LaneCounters& c) {
   const int start = (~code) & kLeafStartMask;
   const int cnt = ((~code) >> kLeafCountShift) + 1;
+  c.tris += (uint32_t)cnt;
   for (int k = 0; k < cnt; ++k) {
     const float4* T = tris + 3 * (start + k);
     const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
@@ -123,7 +128,7 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int c
 // t-range culling so rounding in the slab test never removes a candidate.
 template <bool ANY>
 __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float slack, Hit& h,
-                         bool& budget_hit) {
+                         bool& budget_hit, LaneCounters& c) {
   h.t = tlimit;
   h.pos = -1;
   h.orig = INT_MAX;
@@ -139,6 +144,7 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
       return false;
     }
     const Node* nd = nodes + cur;
+    c.nodes++;
     const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
     const int4 ch = __ldg(&nd->d);
     const float lim = ANY ? tlimit + slack : h.t + (h.t * 2.44140625e-4f + slack);
@@ -146,11 +152,11 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
     if (h0 && ch.x < 0) {
-      if (leaf_test<ANY>(a.tris, ch.x, o, d, h)) return true;
+      if (leaf_test<ANY>(a.tris, ch.x, o, d, h, c)) return true;
       h0 = false;
     }
     if (h1 && ch.y < 0) {
-      if (leaf_test<ANY>(a.tris, ch.y, o, d, h)) return true;
+      if (leaf_test<ANY>(a.tris, ch.y, o, d, h, c)) return true;
       h1 = false;
     }
     if (h0 || h1) {
@@ -218,7 +224,8 @@ struct Track {
 // (src/StereoRecorder.cpp:93) and positions beyond the window.  Groups of
 // four aligned bins go out as one 16-byte vector reduction.
 __device__ __forceinline__ void splat(const Track& tr, int nb, long long s, int w, float ampl,
-                                      float step) {
+                                      float step, uint32_t& bins) {
+  bins += (uint32_t)w;
   const long long lastpos = s + w - 1;
   if (lastpos < 0) return;
   const long long firstpos = s < 0 ? 0 : s;
@@ -268,7 +275,7 @@ __device__ __forceinline__ Track track_of(const TraceArgs& a, int* s_first, int*
 // MonoRecorder::Record / StereoRecorder::Record (src/MonoRecorder.cpp:83-97,
 // src/StereoRecorder.cpp:97-130).
 __device__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir, float amp,
-                       float t, float dist, int* s_first, int* s_last) {
+                       float t, float dist, int* s_first, int* s_last, uint32_t& bins) {
   const float width = f_sqrt(dist);
   const int w = (int)f_ceil(width);
   if (R.channels == 2) {
@@ -284,13 +291,15 @@ __device__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 di
     } else {
       al *= factor * factor;
     }
-    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s_left, w, al, al / (float)w);
+    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s_left, w, al, al / (float)w,
+          bins);
     splat(track_of(a, s_first, s_last, R.track0 + 1, band), a.num_bins, s_right, w, ar,
-          ar / (float)w);
+          ar / (float)w, bins);
   } else {
     const long long s = sample_index(t);
     const float ampl = 2.0f * amp / width;
-    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s, w, ampl, ampl / (float)w);
+    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s, w, ampl, ampl / (float)w,
+          bins);
   }
 }
 
@@ -301,10 +310,6 @@ struct PathState {
   int k;
   int band;
   uint64_t ray;
-};
-
-struct LaneCounters {
-  uint32_t segments, shadow, contrib, overflow;
 };
 
 // Visibility + contribution for every recorder at the current vertex
@@ -322,7 +327,7 @@ __device__ __forceinline__ uint32_t connect_recorders(const TraceArgs& a, const 
     const float len = length(sdir);
     Hit hh;
     const float slack = 2.44140625e-4f + a.box_pad / len;
-    if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, budget_hit)) continue;
+    if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, budget_hit, c)) continue;
     vis |= 1u << (ri & 31);
     const V3 lsdir = normalized(sdir);
     const float dt = k ? dot(lsdir, n) : 1.0f;
@@ -352,7 +357,7 @@ __device__ __forceinline__ uint32_t connect_recorders(const TraceArgs& a, const 
       if (k & 1) I *= -1.0f;
       c.contrib++;
       const float total = st.L + len;
-      record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last);
+      record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last, c.bins);
     }
   }
   return vis;
@@ -421,7 +426,7 @@ __device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats,
   const uint32_t band = (uint32_t)st.band;
   c.segments++;
   Hit h;
-  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, budget_hit);
+  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, budget_hit, c);
   debug_put<DEBUG>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
   const float4 nm = __ldg(a.nrm + h.pos);
@@ -482,7 +487,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  LaneCounters c = {0, 0, 0, 0};
+  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
   bool budget_hit = false;
   bool alive = false, exhausted = false;
   PathState st;
@@ -517,7 +522,13 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
     const uint32_t sh = __reduce_add_sync(kFull, c.shadow);
     const uint32_t co = __reduce_add_sync(kFull, c.contrib);
     const uint32_t ov = __reduce_add_sync(kFull, c.overflow);
+    const unsigned long long nv = __reduce_add_sync(kFull, c.nodes);
+    const unsigned long long tt = __reduce_add_sync(kFull, c.tris);
+    const unsigned long long bn = __reduce_add_sync(kFull, c.bins);
     if (lane == 0) {
+      atomicAdd(a.counters + kNodeVisits, nv);
+      atomicAdd(a.counters + kTriTests, tt);
+      atomicAdd(a.counters + kSplatBins, bn);
       atomicAdd(a.counters + kSegments, (unsigned long long)seg);
       atomicAdd(a.counters + kShadow, (unsigned long long)sh);
       atomicAdd(a.counters + kContrib, (unsigned long long)co);
@@ -550,18 +561,17 @@ __global__ void direct_kernel(const TraceArgs a, float dry) {
   Hit hh;
   const float seglen = length(seg);
   const float slack = 2.44140625e-4f + (seglen > 0.0f ? a.box_pad / seglen : 0.0f);
-  if (traverse<true>(a, loc, seg, 1.0f, slack, hh, budget_hit)) return;
+  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
+  if (traverse<true>(a, loc, seg, 1.0f, slack, hh, budget_hit, c)) return;
   if (budget_hit) atomicOr(a.error_flag, kErrBudget);
   const V3 dist = sub(loc, src);
   const float len = length(dist);
   const V3 dir = normalized(dist);
   const float amp = inv_sphere_2(len) * powf_portable(a.air[band], len) * dry;
+  // first/last live interleaved in the int2 [track][band] array
   int* fl = reinterpret_cast<int*>(a.first_last);
-  // first/last live interleaved as int2 [track][band] -> use strided views
-  int* s_first = fl;      // element (track*3+band)*2
-  int* s_last = fl + 1;   // element (track*3+band)*2 + 1
-  // record() indexes first/last as base + track*3 + band; build per-call
-  // bases with stride 2 by recording through a local shim.
+  int* s_first = fl;
+  int* s_last = fl + 1;
   const float width = f_sqrt(len);
   const int w = (int)f_ceil(width);
   const float t = len / 343.0f;
@@ -585,8 +595,8 @@ __global__ void direct_kernel(const TraceArgs a, float dry) {
     trr.row = a.hist + ((size_t)(R.track0 + 1) * 3 + band) * (size_t)a.stride;
     trr.first = s_first + 2 * ((R.track0 + 1) * 3 + band);
     trr.last = s_last + 2 * ((R.track0 + 1) * 3 + band);
-    splat(tl, a.num_bins, s_left, w, al, al / (float)w);
-    splat(trr, a.num_bins, s_right, w, ar, ar / (float)w);
+    splat(tl, a.num_bins, s_left, w, al, al / (float)w, c.bins);
+    splat(trr, a.num_bins, s_right, w, ar, ar / (float)w, c.bins);
   } else {
     const long long s = sample_index(t);
     const float ampl = 2.0f * amp / width;
@@ -594,7 +604,7 @@ __global__ void direct_kernel(const TraceArgs a, float dry) {
     tm.row = a.hist + ((size_t)R.track0 * 3 + band) * (size_t)a.stride;
     tm.first = s_first + 2 * (R.track0 * 3 + band);
     tm.last = s_last + 2 * (R.track0 * 3 + band);
-    splat(tm, a.num_bins, s, w, ampl, ampl / (float)w);
+    splat(tm, a.num_bins, s, w, ampl, ampl / (float)w, c.bins);
   }
 }
 

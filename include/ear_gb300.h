@@ -94,8 +94,8 @@ typedef struct ear_scene_desc {
 
 typedef struct ear_bvh_opts {
   /* Padding added to every triangle's bounding box, in scene units.  Values
-     < 0 select the default (2^-14 of the largest absolute coordinate plus
-     1e-6).  Padding only makes the culling conservative; it never changes
+     < 0 select the default (2^-12 of the largest absolute coordinate plus
+     1e-5).  Padding only makes the culling conservative; it never changes
      which triangle is reported. */
   float box_pad;
   int32_t reserved[7];
@@ -145,6 +145,9 @@ typedef struct ear_render_stats {
   uint64_t shadow_queries; /* any-hit (visibility) queries */
   uint64_t contributions;  /* valid recorded path contributions */
   uint64_t sampler_overflows; /* rejection loops that reached their bound */
+  uint64_t node_visits;    /* BVH internal-node visits (64 bytes each) */
+  uint64_t triangle_tests; /* ray/triangle tests (48 bytes each) */
+  uint64_t splat_bins;     /* histogram bins written by splats */
   double kernel_ms;        /* device time of the trace kernel(s) */
 } ear_render_stats;
 
