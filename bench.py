@@ -219,7 +219,7 @@ def run_reference(args):
 
 
 def _default_cpu_rays(name):
-    return {"relief_hall": 300, "shoebox": 20000, "cathedral": 4}.get(name, 100)
+    return {"relief_hall": 4000, "shoebox": 20000, "cathedral": 4}.get(name, 100)
 
 
 def _config(w, args, flush):

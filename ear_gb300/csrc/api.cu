@@ -371,6 +371,8 @@ ear_status finish(ear_scene* s, const ear_render_params* p, const Prepared& pr, 
     CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     *kernel_ms = ms;
   }
+  if (errflag & kErrIndex)
+    return fail(EAR_ERR_CUDA, "internal: a device-side index check failed (corrupt BVH or scene data)");
   if (errflag & kErrBudget)
     return fail(EAR_ERR_DEVICE_BUDGET, "a BVH traversal exceeded its iteration budget");
   return EAR_OK;

@@ -114,7 +114,7 @@ enum Counter {
   kSplatBins = 7,   // histogram bins written
   kNumCounters = 8
 };
-enum ErrorBits { kErrBudget = 1 };
+enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 
 // LBVH build (bvh_build.cu).  Returns a cudaError_t; `err` receives a
 // message on failure.

@@ -89,16 +89,28 @@ struct Hit {
   int orig;  // original (file-order) index
 };
 
+// Indices read from device data (child links, parent links, leaf ranges,
+// hit positions, material ids) are range-checked before they address
+// memory; a failed check sets kErrIndex and ends the query instead of
+// touching memory.  One compare per node visit.
+__device__ __forceinline__ bool out_of_range(const TraceArgs& a, unsigned idx, unsigned n) {
+  if (idx < n) return false;
+  atomicOr(a.error_flag, kErrIndex);
+  return true;
+}
+
 struct LaneCounters {
   uint32_t segments, shadow, contrib, overflow, nodes, tris, bins;
 };
 
 // Returns true (ANY) when the segment is blocked.
 template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int code, V3 o, V3 d,
-                                          Hit& h, LaneCounters& c) {
+__device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3 d, Hit& h,
+                                          LaneCounters& c) {
+  const float4* __restrict__ tris = a.tris;
   const int start = (~code) & kLeafStartMask;
   const int cnt = ((~code) >> kLeafCountShift) + 1;
+  if (out_of_range(a, (unsigned)(start + cnt - 1), (unsigned)a.num_tris)) return false;
   c.tris += (uint32_t)cnt;
   for (int k = 0; k < cnt; ++k) {
     const float4* T = tris + 3 * (start + k);
@@ -143,6 +155,7 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
       budget_hit = true;
       return false;
     }
+    if (out_of_range(a, (unsigned)cur, (unsigned)a.num_nodes)) return false;
     const Node* nd = nodes + cur;
     c.nodes++;
     const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
@@ -152,11 +165,11 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
     if (h0 && ch.x < 0) {
-      if (leaf_test<ANY>(a.tris, ch.x, o, d, h, c)) return true;
+      if (leaf_test<ANY>(a, ch.x, o, d, h, c)) return true;
       h0 = false;
     }
     if (h1 && ch.y < 0) {
-      if (leaf_test<ANY>(a.tris, ch.y, o, d, h, c)) return true;
+      if (leaf_test<ANY>(a, ch.y, o, d, h, c)) return true;
       h1 = false;
     }
     if (h0 || h1) {
@@ -175,12 +188,14 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
       if (trail & 1ull) {
         trail ^= 1ull;
         const int par = __ldg(&nodes[cur].d.z);
+        if (out_of_range(a, (unsigned)par, (unsigned)a.num_nodes)) return false;
         const int4 pc = __ldg(&nodes[par].d);
         cur = (pc.x == cur) ? pc.y : pc.x;
         break;
       }
       trail >>= 1;
       cur = __ldg(&nodes[cur].d.z);
+      if (out_of_range(a, (unsigned)cur, (unsigned)a.num_nodes)) return false;
       if (++iters > a.traverse_budget) {
         budget_hit = true;
         return false;
@@ -429,7 +444,9 @@ __device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats,
   traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, budget_hit, c);
   debug_put<DEBUG>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
+  if (out_of_range(a, (unsigned)h.pos, (unsigned)a.num_tris)) return false;
   const float4 nm = __ldg(a.nrm + h.pos);
+  if (out_of_range(a, (unsigned)__float_as_int(nm.w), (unsigned)a.num_mats)) return false;
   const float t = h.t;
   const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
   const V3 N = mk(nm.x, nm.y, nm.z);
@@ -470,7 +487,7 @@ __device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats,
 }
 
 template <bool DEBUG>
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
+__global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevMaterial* s_mats = reinterpret_cast<DevMaterial*>(smem_raw);
   int* s_first = reinterpret_cast<int*>(smem_raw + sizeof(DevMaterial) * a.num_mats);
