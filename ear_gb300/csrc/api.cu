@@ -18,6 +18,7 @@
 
 #include "../../include/ear_gb300.h"
 #include "ear_internal.h"
+#include "ear_record.cuh"
 
 using namespace ear;
 
@@ -40,8 +41,6 @@ ear_status fail(ear_status st, const char* fmt, ...) {
       return fail(e_ == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,  \
                   "%s: %s", #x, cudaGetErrorString(e_));                                  \
   } while (0)
-
-constexpr int kInitialFirstSample = 3 * 44100 - 1;
 
 // Material::Material (src/Material.cpp:26-72) and Material::Bounce
 // (src/Material.cpp:76-83), per band.
@@ -78,17 +77,72 @@ __global__ void k_init_first_last(int2* fl, int n) {
   if (i < n) fl[i] = make_int2(kInitialFirstSample, 0);
 }
 
-// FloatBuffer::Multiply over [first_sample, real_length) of every traced
-// (track, band) row (src/Recorder.cpp:85-89).
-__global__ void k_scale(float* hist, int stride, int nb, int rows, const int2* fl, uint32_t bands,
-                        float f) {
-  const int row = blockIdx.y;
-  if (row >= rows || !((bands >> (row % 3)) & 1u)) return;
-  const int2 r = fl[row];
-  const int hi = r.y < nb ? r.y : nb;
-  float* h = hist + (size_t)row * stride;
-  for (int i = r.x + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
-    h[i] *= f;
+// End of Scene::Render (src/Scene.cpp:286-316) for one (recorder, band),
+// one block each: Recorder::Multiply(1/amount) over every track's
+// [first_sample, real_length) (src/Recorder.cpp:85-89), the direct-sound
+// lobe INV_SPHERE_2(len) * air^len * dry recorded at len / 343 s when the
+// trace kernel found the listener-source segment unblocked, then
+// Multiply(gain^2).  The block owns its rows, so the lobe is added with
+// plain stores by one thread, in the reference's order.
+struct FinalizeArgs {
+  float* hist;
+  int stride;
+  int num_bins;
+  int2* first_last;
+  const DevRecorder* recs;
+  const int* direct_vis;  // null: no direct sound
+  float src[3];
+  float air[3];
+  float dry;
+  float inv_amount;
+  float gain2;
+  uint32_t bands;
+};
+
+__device__ void scale_rows(const FinalizeArgs& f, const DevRecorder& R, int band, float x) {
+  for (int k = 0; k < R.channels; ++k) {
+    const int tb = (R.track0 + k) * 3 + band;
+    const int2 r = f.first_last[tb];
+    const int hi = r.y < f.num_bins ? r.y : f.num_bins;
+    float* h = f.hist + (size_t)tb * f.stride;
+    for (int i = r.x + (int)threadIdx.x; i < hi; i += (int)blockDim.x) h[i] *= x;
+  }
+}
+
+__global__ void k_finalize(const FinalizeArgs f) {
+  const int ri = blockIdx.x / 3, band = blockIdx.x % 3;
+  if (!((f.bands >> band) & 1u)) return;
+  const DevRecorder R = f.recs[ri];
+  scale_rows(f, R, band, f.inv_amount);
+  __syncthreads();
+  if (threadIdx.x == 0 && f.direct_vis && f.direct_vis[ri]) {
+    const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
+    const V3 src = mk(f.src[0], f.src[1], f.src[2]);
+    const V3 dist = sub(loc, src);
+    const float len = length(dist);
+    const V3 dir = normalized(dist);
+    const float amp = inv_sphere_2(len) * powf_portable(f.air[band], len) * f.dry;
+    const SplatPlan p = record_plan(R, band, dir, amp, len / 343.0f, len);
+    for (int k = 0; k < p.tracks; ++k) {
+      const int tb = (R.track0 + k) * 3 + band;
+      float* row = f.hist + (size_t)tb * f.stride;
+      int2 fl = f.first_last[tb];
+      float v = p.ampl[k];
+      for (int i = 0; i < p.w; ++i) {
+        const long long pos = p.s[k] + i;
+        if (pos >= 0) {
+          const int c = (int)(pos < f.num_bins ? pos : f.num_bins);
+          if (c > fl.y) fl.y = c;
+          if (c < fl.x) fl.x = c;
+          if (pos < f.num_bins) row[pos] += v;
+        }
+        v -= p.step[k];
+      }
+      f.first_last[tb] = fl;
+    }
+  }
+  __syncthreads();
+  scale_rows(f, R, band, f.gain2);
 }
 
 }  // namespace
@@ -109,6 +163,8 @@ struct ear_scene {
   size_t counters_cap = 0;
   int* err = nullptr;
   size_t err_cap = 0;
+  int* dvis = nullptr;
+  size_t dvis_cap = 0;
   DevRecorder* recs = nullptr;
   size_t recs_cap = 0;
   float4* emitter = nullptr;
@@ -224,6 +280,7 @@ void ear_scene_destroy(ear_scene* s) {
   cudaFree(s->fl);
   cudaFree(s->counters);
   cudaFree(s->err);
+  cudaFree(s->dvis);
   cudaFree(s->recs);
   cudaFree(s->emitter);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -313,10 +370,14 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   CU(grow(&s->fl, &s->fl_cap, (size_t)std::max(tracks * 3, 1)));
   CU(grow(&s->counters, &s->counters_cap, (size_t)kNumCounters));
   CU(grow(&s->err, &s->err_cap, (size_t)1));
+  CU(grow(&s->dvis, &s->dvis_cap, (size_t)std::max(nrec, 1)));
   CU(grow(&s->hist, &s->hist_cap, (size_t)std::max(tracks * 3, 1) * (size_t)a.stride));
   a.recs = s->recs;
   a.hist = s->hist;
   a.first_last = s->fl;
+  const bool direct = !(p->flags & (EAR_FLAG_RAW | EAR_FLAG_NO_DIRECT)) &&
+                      src->num_emitter_triangles <= 0 && nrec > 0;
+  a.direct_vis = direct ? s->dvis : nullptr;
   a.counters = s->counters;
   a.error_flag = s->err;
   cudaStream_t st = (cudaStream_t)p->stream;
@@ -392,23 +453,30 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
   TraceArgs& a = pr.a;
   cudaStream_t st = (cudaStream_t)p->stream;
   CU(cudaEventRecord(s->ev0, st));
-  if (a.num_items > 0) CU(pr.ops->trace(a, pr.grid, pr.smem, false, st));
+  // with no rays the launch still computes the direct-sound visibility
+  CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.smem, false, st));
   CU(cudaEventRecord(s->ev1, st));
   const int rows = pr.num_tracks * 3;
-  if (!(p->flags & EAR_FLAG_RAW) && rows > 0) {
-    // src/Scene.cpp:286-316: Multiply(1/amount), direct sound, Multiply(gain^2).
-    // amount is a float incremented once per ray: exact to 2^24, then stuck.
+  if (!(p->flags & EAR_FLAG_RAW) && nrec > 0) {
+    // amount is a float incremented once per ray (src/Scene.cpp:122,127):
+    // exact to 2^24 rays, then stuck at 2^24.
     const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
-    const float inv_amount = 1.0f / amount;
-    const float gain2 = src->gain * src->gain;
-    const dim3 grid((unsigned)std::min(1024, (a.num_bins + 255) / 256), (unsigned)rows);
-    k_scale<<<grid, 256, 0, st>>>(a.hist, a.stride, a.num_bins, rows, a.first_last, p->bands_mask,
-                                  inv_amount);
-    CU(cudaGetLastError());
-    if (src->num_emitter_triangles <= 0 && !(p->flags & EAR_FLAG_NO_DIRECT))
-      CU(pr.ops->direct(a, p->dry_level, st));
-    k_scale<<<grid, 256, 0, st>>>(a.hist, a.stride, a.num_bins, rows, a.first_last, p->bands_mask,
-                                  gain2);
+    FinalizeArgs f;
+    f.hist = a.hist;
+    f.stride = a.stride;
+    f.num_bins = a.num_bins;
+    f.first_last = a.first_last;
+    f.recs = a.recs;
+    f.direct_vis = a.direct_vis;
+    for (int k = 0; k < 3; ++k) {
+      f.src[k] = a.src[k];
+      f.air[k] = a.air[k];
+    }
+    f.dry = p->dry_level;
+    f.inv_amount = 1.0f / amount;
+    f.gain2 = src->gain * src->gain;
+    f.bands = p->bands_mask;
+    k_finalize<<<nrec * 3, 256, 0, st>>>(f);
     CU(cudaGetLastError());
   }
   if (rows > 0) {

@@ -91,6 +91,7 @@ struct TraceArgs {
   int num_bins;
   int num_tracks;
   int2* first_last;  // [track][band]
+  int* direct_vis;   // [recorder] direct-path visibility, or null
   unsigned long long* counters;  // [0] work, [1] segments, [2] shadow, [3] contrib, [4] overflow
   int* error_flag;
   int traverse_budget;
@@ -123,7 +124,6 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char*
 // Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
 struct TraceOps {
   cudaError_t (*trace)(const TraceArgs& a, int grid, size_t smem, bool debug, cudaStream_t s);
-  cudaError_t (*direct)(const TraceArgs& a, float dry, cudaStream_t s);
   cudaError_t (*occupancy)(bool debug, size_t smem, int* blocks_per_sm);
   int block;
 };

@@ -19,13 +19,6 @@ cudaError_t trace_exact(const TraceArgs& a, int grid, size_t smem, bool debug, c
   return cudaGetLastError();
 }
 
-cudaError_t direct_exact(const TraceArgs& a, float dry, cudaStream_t s) {
-  const int n = a.num_recs * 3;
-  if (n == 0) return cudaSuccess;
-  exact::direct_kernel<<<(n + 63) / 64, 64, 0, s>>>(a, dry);
-  return cudaGetLastError();
-}
-
 cudaError_t occupancy_exact(bool debug, size_t smem, int* blocks_per_sm) {
   if (debug) {
     cudaFuncSetAttribute(exact::trace_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -41,6 +34,6 @@ cudaError_t occupancy_exact(bool debug, size_t smem, int* blocks_per_sm) {
 
 }  // namespace
 
-const TraceOps kTraceExact = {trace_exact, direct_exact, occupancy_exact, exact::kTraceBlock};
+const TraceOps kTraceExact = {trace_exact, occupancy_exact, exact::kTraceBlock};
 
 }  // namespace ear

@@ -19,13 +19,6 @@ cudaError_t trace_fast(const TraceArgs& a, int grid, size_t smem, bool debug, cu
   return cudaGetLastError();
 }
 
-cudaError_t direct_fast(const TraceArgs& a, float dry, cudaStream_t s) {
-  const int n = a.num_recs * 3;
-  if (n == 0) return cudaSuccess;
-  fast::direct_kernel<<<(n + 63) / 64, 64, 0, s>>>(a, dry);
-  return cudaGetLastError();
-}
-
 cudaError_t occupancy_fast(bool debug, size_t smem, int* blocks_per_sm) {
   if (debug) {
     cudaFuncSetAttribute(fast::trace_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -41,6 +34,6 @@ cudaError_t occupancy_fast(bool debug, size_t smem, int* blocks_per_sm) {
 
 }  // namespace
 
-const TraceOps kTraceFast = {trace_fast, direct_fast, occupancy_fast, fast::kTraceBlock};
+const TraceOps kTraceFast = {trace_fast, occupancy_fast, fast::kTraceBlock};
 
 }  // namespace ear

@@ -10,7 +10,8 @@
 // (closest hit, material choice, new direction, R visibility queries and
 // splats).  Lanes whose path ended are refilled from a global work counter
 // with one atomic per warp (ballot + popc + shuffle), so warps stay full
-// while path lengths vary from 1 to max_bounces.  BVH traversal is
+// while path lengths vary from 1 to max_bounces.  Warps reconverge
+// (__syncwarp) after every data-dependent loop.  BVH traversal is
 // stackless: a 64-bit trail records, per level of the current root path,
 // whether the far child is still pending; backtracking climbs parent links.
 #pragma once
@@ -22,13 +23,13 @@
 #include <limits.h>
 
 #include "ear_internal.h"
+#include "ear_record.cuh"
 
 namespace ear {
 namespace EAR_NS {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTraceBlock = 256;
-constexpr int kInitialFirstSample = 3 * 44100 - 1;  // src/Recorder.cpp:46
 
 struct Ray {
   float ox, oy, oz;
@@ -89,37 +90,42 @@ struct Hit {
   int orig;  // original (file-order) index
 };
 
-// Indices read from device data (child links, parent links, leaf ranges,
-// hit positions, material ids) are range-checked before they address
-// memory; a failed check sets kErrIndex and ends the query instead of
-// touching memory.  One compare per node visit.
-__device__ __forceinline__ bool out_of_range(const TraceArgs& a, unsigned idx, unsigned n) {
-  if (idx < n) return false;
-  atomicOr(a.error_flag, kErrIndex);
-  return true;
-}
-
 struct LaneCounters {
   uint32_t segments, shadow, contrib, overflow, nodes, tris, bins;
 };
 
+// Indices read from device data (child and parent links, leaf ranges, hit
+// positions, material ids) are range-checked before they address memory.
+// A failed check sets kErrIndex in `err` and clamps the index to 0 -- no
+// early exit, so the warp keeps its shape; the launch then fails with
+// EAR_ERR_CUDA instead of touching memory outside the scene.
+__device__ __forceinline__ int clamp_index(int idx, int n, int& err) {
+  const bool b = (unsigned)idx >= (unsigned)n;
+  if (b) err |= kErrIndex;
+  return b ? 0 : idx;
+}
+
 // Returns true (ANY) when the segment is blocked.
 template <bool ANY>
 __device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3 d, Hit& h,
-                                          LaneCounters& c) {
-  const float4* __restrict__ tris = a.tris;
-  const int start = (~code) & kLeafStartMask;
-  const int cnt = ((~code) >> kLeafCountShift) + 1;
-  if (out_of_range(a, (unsigned)(start + cnt - 1), (unsigned)a.num_tris)) return false;
+                                          LaneCounters& c, int& err) {
+  int start = (~code) & kLeafStartMask;
+  int cnt = ((~code) >> kLeafCountShift) + 1;
+  if ((unsigned)(start + cnt - 1) >= (unsigned)a.num_tris) {
+    err |= kErrIndex;
+    start = 0;
+    cnt = 1;
+  }
   c.tris += (uint32_t)cnt;
+  bool blocked = false;
   for (int k = 0; k < cnt; ++k) {
-    const float4* T = tris + 3 * (start + k);
+    const float4* T = a.tris + 3 * (start + k);
     const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
     float t;
     if (mt_intersect(A, B, C, o, d, t)) {
       if (ANY) {
         // Mesh::LineIntersection: 1e-5 < t < 1 (src/Mesh.cpp:65)
-        if (t > 1e-5f && t < 1.0f) return true;
+        blocked |= (t > 1e-5f && t < 1.0f);
       } else {
         // Mesh::RayIntersection: t > 0.001, strict t < d, lowest index on
         // ties (src/Mesh.cpp:40) == lexicographic min of (t, index).
@@ -132,7 +138,7 @@ __device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3
       }
     }
   }
-  return false;
+  return blocked;
 }
 
 // Stackless traversal.  Closest hit (ANY = false): h receives the hit.
@@ -140,7 +146,7 @@ __device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3
 // t-range culling so rounding in the slab test never removes a candidate.
 template <bool ANY>
 __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float slack, Hit& h,
-                         bool& budget_hit, LaneCounters& c) {
+                         LaneCounters& c, int& err) {
   h.t = tlimit;
   h.pos = -1;
   h.orig = INT_MAX;
@@ -150,12 +156,14 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
   unsigned long long trail = 1ull;
   int iters = 0;
   const Node* __restrict__ nodes = a.nodes;
+  bool blocked = false;
+  const int err0 = err;
   for (;;) {
     if (++iters > a.traverse_budget) {
-      budget_hit = true;
-      return false;
+      err |= kErrBudget;
+      break;
     }
-    if (out_of_range(a, (unsigned)cur, (unsigned)a.num_nodes)) return false;
+    cur = clamp_index(cur, a.num_nodes, err);
     const Node* nd = nodes + cur;
     c.nodes++;
     const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
@@ -165,13 +173,14 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
     if (h0 && ch.x < 0) {
-      if (leaf_test<ANY>(a, ch.x, o, d, h, c)) return true;
+      blocked |= leaf_test<ANY>(a, ch.x, o, d, h, c, err);
       h0 = false;
     }
     if (h1 && ch.y < 0) {
-      if (leaf_test<ANY>(a, ch.y, o, d, h, c)) return true;
+      blocked |= leaf_test<ANY>(a, ch.y, o, d, h, c, err);
       h1 = false;
     }
+    if (ANY && blocked) break;
     if (h0 || h1) {
       if (h0 && h1) {
         trail = (trail << 1) | 1ull;
@@ -183,25 +192,34 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
       continue;
     }
     // backtrack to the deepest level whose far child is pending
+    bool done = false;
     for (;;) {
-      if (trail == 1ull) return false;
+      if (trail == 1ull) {
+        done = true;
+        break;
+      }
       if (trail & 1ull) {
         trail ^= 1ull;
-        const int par = __ldg(&nodes[cur].d.z);
-        if (out_of_range(a, (unsigned)par, (unsigned)a.num_nodes)) return false;
+        const int par = clamp_index(__ldg(&nodes[cur].d.z), a.num_nodes, err);
         const int4 pc = __ldg(&nodes[par].d);
         cur = (pc.x == cur) ? pc.y : pc.x;
         break;
       }
       trail >>= 1;
-      cur = __ldg(&nodes[cur].d.z);
-      if (out_of_range(a, (unsigned)cur, (unsigned)a.num_nodes)) return false;
+      cur = clamp_index(__ldg(&nodes[cur].d.z), a.num_nodes, err);
       if (++iters > a.traverse_budget) {
-        budget_hit = true;
-        return false;
+        err |= kErrBudget;
+        done = true;
+        break;
       }
     }
+    if (done) break;
   }
+  if (err != err0) {
+    h.pos = -1;
+    return false;
+  }
+  return blocked;
 }
 
 // ------------------------------------------------------------- sampling
@@ -210,6 +228,8 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
 // material choice).
 __device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t band, uint64_t ray,
                                            uint32_t bounce, bool hemi, V3 n, U4 b, V3& out) {
+  bool ok = false;
+  out = mk(0.0f, 0.0f, 1.0f);
   for (int tr = 0; tr < kMaxTries; ++tr) {
     if (tr) b = rng_block(a.k0, a.k1, a.context, band, ray, 0, bounce, (uint32_t)tr);
     const float f1 = uniform24(b.x) * 2.0f - 1.0f;
@@ -221,41 +241,38 @@ __device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t band, ui
     const V3 v = mk(f1 / sl, f2 / sl, f3 / sl);
     if (hemi && dot(n, v) < 0.0f) continue;
     out = v;
-    return true;
+    ok = true;
+    break;
   }
-  out = mk(0.0f, 0.0f, 1.0f);
-  return false;
+  return ok;
 }
 
 // ---------------------------------------------------------------- splats
-struct Track {
-  float* row;
-  int* first;  // shared-memory bookkeeping of this (track, band)
-  int* last;
-};
-
 // Adds the triangular splat v_0 = ampl, v_{i+1} = v_i - step at positions
 // s .. s+w-1 (src/MonoRecorder.cpp:90-93), skipping negative positions
-// (src/StereoRecorder.cpp:93) and positions beyond the window.  Groups of
-// four aligned bins go out as one 16-byte vector reduction.
-__device__ __forceinline__ void splat(const Track& tr, int nb, long long s, int w, float ampl,
-                                      float step, uint32_t& bins) {
+// (src/StereoRecorder.cpp:93) and positions beyond the window, and updates
+// the FloatBuffer bookkeeping (first_sample / real_length,
+// src/Recorder.cpp:56-57) in shared memory.  Groups of four aligned bins go
+// out as one 16-byte vector reduction.
+__device__ __forceinline__ void splat(float* row, int* first, int* last, int nb, long long s,
+                                      int w, float ampl, float step, uint32_t& bins) {
   bins += (uint32_t)w;
   const long long lastpos = s + w - 1;
   if (lastpos < 0) return;
   const long long firstpos = s < 0 ? 0 : s;
-  atomicMin(tr.first, (int)(firstpos < nb ? firstpos : nb));
-  atomicMax(tr.last, (int)(lastpos < nb ? lastpos : nb));
+  atomicMin(first, (int)(firstpos < nb ? firstpos : nb));
+  atomicMax(last, (int)(lastpos < nb ? lastpos : nb));
   if (firstpos >= nb) return;
   float v = ampl;
   float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   int grp = -1;
   for (int i = 0; i < w; ++i) {
     const long long pos = s + i;
-    if (pos >= 0 && pos < nb) {
+    if (pos >= nb) break;
+    if (pos >= 0) {
       const int g = (int)(pos >> 2);
       if (g != grp) {
-        if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(tr.row + 4 * grp), acc);
+        if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(row + 4 * grp), acc);
         acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         grp = g;
       }
@@ -267,54 +284,17 @@ __device__ __forceinline__ void splat(const Track& tr, int nb, long long s, int 
     }
     v -= step;
   }
-  if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(tr.row + 4 * grp), acc);
+  if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(row + 4 * grp), acc);
 }
 
-// (int)(t * 44100.0) in double as the reference does; values that do not
-// fit an int are treated as beyond the window.
-__device__ __forceinline__ long long sample_index(float t) {
-  const double ts = (double)t * 44100.0;
-  if (!(ts < 2147483647.0) || !(ts > -2147483648.0)) return (long long)1 << 40;
-  return (long long)(int)ts;
-}
-
-__device__ __forceinline__ Track track_of(const TraceArgs& a, int* s_first, int* s_last,
-                                          int track, int band) {
-  Track tr;
-  tr.row = a.hist + ((size_t)track * 3 + band) * (size_t)a.stride;
-  tr.first = s_first + track * 3 + band;
-  tr.last = s_last + track * 3 + band;
-  return tr;
-}
-
-// MonoRecorder::Record / StereoRecorder::Record (src/MonoRecorder.cpp:83-97,
-// src/StereoRecorder.cpp:97-130).
-__device__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir, float amp,
-                       float t, float dist, int* s_first, int* s_last, uint32_t& bins) {
-  const float width = f_sqrt(dist);
-  const int w = (int)f_ceil(width);
-  if (R.channels == 2) {
-    const float dt = dot(dir, mk(R.right[0], R.right[1], R.right[2]));
-    const float time_difference = R.head_size / 343.0f;
-    const long long s_right = sample_index(t - (dt * time_difference));
-    const long long s_left = sample_index(t + (dt * time_difference));
-    const float ampl = 2.0f * amp / width;
-    float al = ampl, ar = ampl;
-    const float factor = powf_portable(R.habs[band], f_abs(dt) * R.head_size);
-    if (dt < 0) {
-      ar *= factor * factor;
-    } else {
-      al *= factor * factor;
-    }
-    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s_left, w, al, al / (float)w,
-          bins);
-    splat(track_of(a, s_first, s_last, R.track0 + 1, band), a.num_bins, s_right, w, ar,
-          ar / (float)w, bins);
-  } else {
-    const long long s = sample_index(t);
-    const float ampl = 2.0f * amp / width;
-    splat(track_of(a, s_first, s_last, R.track0, band), a.num_bins, s, w, ampl, ampl / (float)w,
-          bins);
+__device__ __forceinline__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir,
+                                       float amp, float t, float dist, int* s_first, int* s_last,
+                                       uint32_t& bins) {
+  const SplatPlan p = record_plan(R, band, dir, amp, t, dist);
+  for (int k = 0; k < p.tracks; ++k) {
+    const int tb = (R.track0 + k) * 3 + band;
+    splat(a.hist + (size_t)tb * (size_t)a.stride, s_first + tb, s_last + tb, a.num_bins, p.s[k],
+          p.w, p.ampl[k], p.step[k], bins);
   }
 }
 
@@ -327,55 +307,60 @@ struct PathState {
   uint64_t ray;
 };
 
-// Visibility + contribution for every recorder at the current vertex
-// (src/Scene.cpp:185-270).  bt: 0 REFLECT, 1 REFRACT.
-__device__ __forceinline__ uint32_t connect_recorders(const TraceArgs& a, const PathState& st,
-                                                      V3 n, int bt, float spec_coef, float before,
-                                                      LaneCounters& c, bool& budget_hit,
-                                                      int* s_first, int* s_last) {
-  uint32_t vis = 0;
+// The state a vertex hands to the recorder phase.
+struct Vertex {
+  V3 n;          // oriented (and, for REFRACT, flipped) surface normal
+  int bt;        // 0 REFLECT, 1 REFRACT (src/Material.h:27)
+  float spec;    // specularity of the hit material in this band
+  float before;  // sample_intensity_before_bounce (src/Scene.cpp:173)
+  bool conn;     // connect the recorders at this vertex
+};
+
+// Visibility + contribution of recorder `ri` at the current vertex
+// (src/Scene.cpp:188-268).  Returns whether the recorder is visible.
+__device__ __forceinline__ bool connect_one(const TraceArgs& a, const PathState& st,
+                                            const Vertex& vx, int ri, LaneCounters& c, int& err,
+                                            int* s_first, int* s_last) {
+  const DevRecorder& R = a.recs[ri];
+  const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
+  c.shadow++;
+  const float len = length(sdir);
+  Hit hh;
+  const float slack = 2.44140625e-4f + a.box_pad / len;
+  if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
   const int k = st.k;
-  for (int ri = 0; ri < a.num_recs; ++ri) {
-    const DevRecorder& R = a.recs[ri];
-    const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
-    c.shadow++;
-    const float len = length(sdir);
-    Hit hh;
-    const float slack = 2.44140625e-4f + a.box_pad / len;
-    if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, budget_hit, c)) continue;
-    vis |= 1u << (ri & 31);
-    const V3 lsdir = normalized(sdir);
-    const float dt = k ? dot(lsdir, n) : 1.0f;
-    if (!(dt > 0)) continue;
-    float I = before;
-    if (k) {
-      float factor;
-      if (bt == 0) {
-        const V3 refl_vector = reflect(st.prev, n);
-        const float diff_factor = -dot(n, st.prev);
-        const float rv = dot(refl_vector, lsdir);
-        const float spec_factor = (0.0f < rv) ? rv : 0.0f;
-        factor = spec_coef * 1001.0f * powf_portable(spec_factor, 1000.0f) +
-                 (1.0f - spec_coef) * diff_factor;
-      } else {
-        const float diff_factor = dot(n, st.prev);
-        const float rv = dot(st.prev, lsdir);
-        const float spec_factor = (0.0f < rv) ? rv : 0.0f;
-        factor = spec_coef * 1001.0f * powf_portable(spec_factor, 1000.0f) +
-                 (1.0f - spec_coef) * diff_factor;
-      }
-      I *= factor;
+  const V3 lsdir = normalized(sdir);
+  const float dt = k ? dot(lsdir, vx.n) : 1.0f;
+  if (!(dt > 0)) return true;
+  float I = vx.before;
+  if (k) {
+    const V3 n = vx.n;
+    float factor;
+    if (vx.bt == 0) {
+      const V3 refl_vector = reflect(st.prev, n);
+      const float diff_factor = -dot(n, st.prev);
+      const float rv = dot(refl_vector, lsdir);
+      const float spec_factor = (0.0f < rv) ? rv : 0.0f;
+      factor = vx.spec * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+               (1.0f - vx.spec) * diff_factor;
+    } else {
+      const float diff_factor = dot(n, st.prev);
+      const float rv = dot(st.prev, lsdir);
+      const float spec_factor = (0.0f < rv) ? rv : 0.0f;
+      factor = vx.spec * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+               (1.0f - vx.spec) * diff_factor;
     }
-    I *= powf_portable(a.air[st.band], len);
-    I *= inv_hemi_2(len);
-    if (!invalid_float(I)) {
-      if (k & 1) I *= -1.0f;
-      c.contrib++;
-      const float total = st.L + len;
-      record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last, c.bins);
-    }
+    I *= factor;
   }
-  return vis;
+  I *= powf_portable(a.air[st.band], len);
+  I *= inv_hemi_2(len);
+  if (!invalid_float(I)) {
+    if (k & 1) I *= -1.0f;
+    c.contrib++;
+    const float total = st.L + len;
+    record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last, c.bins);
+  }
+  return true;
 }
 
 template <bool DEBUG>
@@ -390,11 +375,9 @@ __device__ __forceinline__ void debug_put(const TraceArgs& a, const PathState& s
   if (what == 2) a.dbg_vis[i] = vis;
 }
 
-// Bounce 0: AbstractSoundFile::SoundRay (src/SoundFile.cpp:215-228) and,
-// for area emitters, the bounce-0 connections (src/Scene.cpp:185).
-// Returns whether the path continues.
-__device__ bool emit(const TraceArgs& a, PathState& st, LaneCounters& c, bool& budget_hit,
-                     int* s_first, int* s_last) {
+// Bounce 0: AbstractSoundFile::SoundRay (src/SoundFile.cpp:215-228).  Area
+// emitters connect the recorders at bounce 0 (src/Scene.cpp:185).
+__device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, Vertex& vx) {
   st.I = 1.0f;
   st.L = 0.0f;
   st.k = 0;
@@ -422,36 +405,36 @@ __device__ bool emit(const TraceArgs& a, PathState& st, LaneCounters& c, bool& b
     }
     st.o = p;
     if (!sample_dir(a, band, st.ray, 0, true, en, b0, st.d)) c.overflow++;
-    // bounce-0 connections of a mesh source, intensity 1
-    connect_recorders(a, st, mk(0, 0, 0), 0, 0.0f, st.I, c, budget_hit, s_first, s_last);
   } else {
     st.o = mk(a.src[0], a.src[1], a.src[2]);
     if (!sample_dir(a, band, st.ray, 0, false, mk(0, 0, 0), b0, st.d)) c.overflow++;
   }
-  if ((double)st.I < a.cutoff) return false;
-  st.prev = normalized(st.d);
-  return a.max_bounces > 0;
+  vx.n = mk(0, 0, 0);
+  vx.bt = 0;
+  vx.spec = 0.0f;
+  vx.before = st.I;
+  vx.conn = a.num_emitter > 0;
 }
 
-// One reflection k = st.k + 1 (src/Scene.cpp:150-280).
+// Reflection k = st.k + 1 up to the recorder connections
+// (src/Scene.cpp:150-177): closest hit, Material::Bounce, Sample_Hemi,
+// air and surface losses.  Returns whether the path continues.
 template <bool DEBUG>
-__device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats, PathState& st,
-                       LaneCounters& c, bool& budget_hit, int* s_first, int* s_last) {
+__device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict__ mats,
+                              PathState& st, LaneCounters& c, int& err, Vertex& vx) {
   const int k = st.k + 1;
   const uint32_t band = (uint32_t)st.band;
   c.segments++;
   Hit h;
-  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, budget_hit, c);
+  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, c, err);
   debug_put<DEBUG>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
-  if (out_of_range(a, (unsigned)h.pos, (unsigned)a.num_tris)) return false;
   const float4 nm = __ldg(a.nrm + h.pos);
-  if (out_of_range(a, (unsigned)__float_as_int(nm.w), (unsigned)a.num_mats)) return false;
   const float t = h.t;
   const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
   const V3 N = mk(nm.x, nm.y, nm.z);
   V3 n = (dot(N, st.d) > 0.0f) ? neg(N) : N;
-  const DevMaterial& M = mats[__float_as_int(nm.w)];
+  const DevMaterial& M = mats[clamp_index(__float_as_int(nm.w), a.num_mats, err)];
   // Material::Bounce (src/Material.cpp:76-83)
   const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, (uint32_t)k, 0);
   int bt = 0;
@@ -476,18 +459,34 @@ __device__ bool bounce(const TraceArgs& a, const DevMaterial* __restrict__ mats,
   st.d = v;
   st.k = k;
   st.I *= M.survival[band];
-  const float before = st.I;
-  if (invalid_float(st.I)) return false;
-  const uint32_t vis =
-      connect_recorders(a, st, n, bt, spec, before, c, budget_hit, s_first, s_last);
-  debug_put<DEBUG>(a, st, k, 0, 0, vis, 2);
-  if ((double)st.I < a.cutoff) return false;
-  st.prev = normalized(st.d);
-  return k < a.max_bounces;
+  vx.n = n;
+  vx.bt = bt;
+  vx.spec = spec;
+  vx.before = st.I;
+  vx.conn = true;
+  return !invalid_float(st.I);
+}
+
+// Direct-sound visibility (src/Scene.cpp:299-304): Connect(listener,
+// source) for every recorder, computed by the first threads of block 0
+// with the same any-hit traversal as the path connections.  The lobe
+// itself is added by the finalize kernel between the two scaling passes.
+__device__ void direct_visibility(const TraceArgs& a, int& err) {
+  const int r = (int)threadIdx.x;
+  if (blockIdx.x != 0 || r >= a.num_recs || a.direct_vis == nullptr) return;
+  const DevRecorder& R = a.recs[r];
+  const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
+  const V3 seg = sub(mk(a.src[0], a.src[1], a.src[2]), loc);
+  const float seglen = length(seg);
+  const float slack = 2.44140625e-4f + (seglen > 0.0f ? a.box_pad / seglen : 0.0f);
+  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
+  Hit hh;
+  const bool blocked = traverse<true>(a, loc, seg, 1.0f, slack, hh, c, err);
+  a.direct_vis[r] = blocked ? 0 : 1;
 }
 
 template <bool DEBUG>
-__global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a) {
+__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevMaterial* s_mats = reinterpret_cast<DevMaterial*>(smem_raw);
   int* s_first = reinterpret_cast<int*>(smem_raw + sizeof(DevMaterial) * a.num_mats);
@@ -502,17 +501,23 @@ __global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a
       s_last[i] = 0;
     }
   }
+  int err = 0;
+  direct_visibility(a, err);
   __syncthreads();
   const int lane = threadIdx.x & 31;
   LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
-  bool budget_hit = false;
   bool alive = false, exhausted = false;
   PathState st;
   st.k = 0;
   st.band = 0;
   st.ray = 0;
+  // Every lane, live or not, passes the same __syncwarp() points below;
+  // per-lane work between them is predicated, so divergent loops
+  // (traversal, rejection sampling) reconverge at each phase boundary.
   for (;;) {
+    // phase 1: refill lanes whose path ended (one atomic per warp)
     const unsigned need = __ballot_sync(kFull, !alive && !exhausted);
+    bool fresh = false;
     if (need) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
@@ -522,17 +527,44 @@ __global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a
         const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
         if (w < a.num_items) {
           const uint64_t bi = w / a.num_rays;
-          st.band = a.bands[bi];
+          st.band = a.bands[bi < 3 ? bi : 0];
           st.ray = w - bi * a.num_rays;
-          alive = emit(a, st, c, budget_hit, s_first, s_last);
+          fresh = true;
         } else {
           exhausted = true;
         }
       }
     }
     if (__all_sync(kFull, exhausted)) break;
-    if (alive) alive = bounce<DEBUG>(a, s_mats, st, c, budget_hit, s_first, s_last);
+    // phase 2: one path vertex -- the emission of a fresh ray or the next
+    // reflection of a live one
+    Vertex vx;
+    vx.conn = false;
+    if (fresh) {
+      emit_vertex(a, st, c, vx);
+      alive = true;
+    } else if (alive) {
+      alive = bounce_vertex<DEBUG>(a, s_mats, st, c, err, vx);
+      vx.conn = alive;
+    }
+    __syncwarp();
+    // phase 3: recorder connections (src/Scene.cpp:185-270)
+    uint32_t vis = 0;
+    for (int ri = 0; ri < a.num_recs; ++ri) {
+      if (vx.conn && connect_one(a, st, vx, ri, c, err, s_first, s_last)) vis |= 1u << (ri & 31);
+      __syncwarp();
+    }
+    // phase 4: cut-off, next direction, bounce limit (src/Scene.cpp:275-277)
+    if (alive) {
+      if (st.k > 0) debug_put<DEBUG>(a, st, st.k, 0, 0, vis, 2);
+      if ((double)st.I < a.cutoff || st.k >= a.max_bounces) {
+        alive = false;
+      } else {
+        st.prev = normalized(st.d);
+      }
+    }
   }
+  __syncwarp();
   // flush statistics: one atomic per warp and counter
   {
     const uint32_t seg = __reduce_add_sync(kFull, c.segments);
@@ -542,6 +574,7 @@ __global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a
     const unsigned long long nv = __reduce_add_sync(kFull, c.nodes);
     const unsigned long long tt = __reduce_add_sync(kFull, c.tris);
     const unsigned long long bn = __reduce_add_sync(kFull, c.bins);
+    const int werr = (int)__reduce_or_sync(kFull, (unsigned)err);
     if (lane == 0) {
       atomicAdd(a.counters + kNodeVisits, nv);
       atomicAdd(a.counters + kTriTests, tt);
@@ -550,78 +583,13 @@ __global__ void __launch_bounds__(kTraceBlock, 2) trace_kernel(const TraceArgs a
       atomicAdd(a.counters + kShadow, (unsigned long long)sh);
       atomicAdd(a.counters + kContrib, (unsigned long long)co);
       if (ov) atomicAdd(a.counters + kOverflow, (unsigned long long)ov);
+      if (werr) atomicOr(a.error_flag, werr);
     }
-    if (__any_sync(kFull, budget_hit) && lane == 0) atomicOr(a.error_flag, kErrBudget);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
     if (s_last[i] > 0) atomicMax(&a.first_last[i].y, s_last[i]);
     if (s_first[i] < kInitialFirstSample) atomicMin(&a.first_last[i].x, s_first[i]);
-  }
-}
-
-// End of Scene::Render (src/Scene.cpp:286-316), part 2: the direct-sound
-// lobe, one thread per (recorder, band).  Runs between the two scaling
-// passes; writes go straight to the rows with first/last in global memory.
-__global__ void direct_kernel(const TraceArgs a, float dry) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.num_recs * 3) return;
-  const int ri = i / 3, band = i % 3;
-  bool on = false;
-  for (int b = 0; b < 3; ++b) on |= (a.bands[b] == band);
-  if (!on) return;
-  const DevRecorder& R = a.recs[ri];
-  const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
-  const V3 src = mk(a.src[0], a.src[1], a.src[2]);
-  const V3 seg = sub(src, loc);
-  bool budget_hit = false;
-  Hit hh;
-  const float seglen = length(seg);
-  const float slack = 2.44140625e-4f + (seglen > 0.0f ? a.box_pad / seglen : 0.0f);
-  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
-  if (traverse<true>(a, loc, seg, 1.0f, slack, hh, budget_hit, c)) return;
-  if (budget_hit) atomicOr(a.error_flag, kErrBudget);
-  const V3 dist = sub(loc, src);
-  const float len = length(dist);
-  const V3 dir = normalized(dist);
-  const float amp = inv_sphere_2(len) * powf_portable(a.air[band], len) * dry;
-  // first/last live interleaved in the int2 [track][band] array
-  int* fl = reinterpret_cast<int*>(a.first_last);
-  int* s_first = fl;
-  int* s_last = fl + 1;
-  const float width = f_sqrt(len);
-  const int w = (int)f_ceil(width);
-  const float t = len / 343.0f;
-  if (R.channels == 2) {
-    const float dt = dot(dir, mk(R.right[0], R.right[1], R.right[2]));
-    const float time_difference = R.head_size / 343.0f;
-    const long long s_right = sample_index(t - (dt * time_difference));
-    const long long s_left = sample_index(t + (dt * time_difference));
-    const float ampl = 2.0f * amp / width;
-    float al = ampl, ar = ampl;
-    const float factor = powf_portable(R.habs[band], f_abs(dt) * R.head_size);
-    if (dt < 0) {
-      ar *= factor * factor;
-    } else {
-      al *= factor * factor;
-    }
-    Track tl, trr;
-    tl.row = a.hist + ((size_t)R.track0 * 3 + band) * (size_t)a.stride;
-    tl.first = s_first + 2 * (R.track0 * 3 + band);
-    tl.last = s_last + 2 * (R.track0 * 3 + band);
-    trr.row = a.hist + ((size_t)(R.track0 + 1) * 3 + band) * (size_t)a.stride;
-    trr.first = s_first + 2 * ((R.track0 + 1) * 3 + band);
-    trr.last = s_last + 2 * ((R.track0 + 1) * 3 + band);
-    splat(tl, a.num_bins, s_left, w, al, al / (float)w, c.bins);
-    splat(trr, a.num_bins, s_right, w, ar, ar / (float)w, c.bins);
-  } else {
-    const long long s = sample_index(t);
-    const float ampl = 2.0f * amp / width;
-    Track tm;
-    tm.row = a.hist + ((size_t)R.track0 * 3 + band) * (size_t)a.stride;
-    tm.first = s_first + 2 * (R.track0 * 3 + band);
-    tm.last = s_last + 2 * (R.track0 * 3 + band);
-    splat(tm, a.num_bins, s, w, ampl, ampl / (float)w, c.bins);
   }
 }
 
