@@ -95,6 +95,9 @@ SIGNATURES = {
     "ear_trace_debug": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
                                   C.c_int32, C.POINTER(EarRenderParams), C.c_int32, C.c_int32,
                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ear_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
+                                     C.c_int32, C.POINTER(EarRenderParams), C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.POINTER(EarRenderStats)]),
     "ear_track_power": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),
     "ear_track_maximum": (C.c_float, [C.c_void_p, C.c_int32, C.c_int32]),
     "ear_track_multiply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),

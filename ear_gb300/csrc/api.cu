@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/ear_gb300.h"
@@ -660,3 +661,207 @@ ear_status ear_statistical_t60(const float* vertices, const int64_t* block_trian
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// ear_render_noalloc: ear_render for callers that must not allocate.
+//
+// Everything the render needs beyond the caller's inputs and outputs (the
+// recorder table, the FloatBuffer first/last bookkeeping, the path
+// counters, the error flag and the direct-sound visibility flags) lives in
+// one file-scope device array, so a call makes no cudaMalloc / cudaFree and
+// no host heap allocation.  Histograms accumulate straight into the
+// caller's device buffer.
+namespace {
+
+constexpr int kNoAllocScratchBytes = 16384;
+constexpr size_t kNaCounters = 0;      // 8 x u64 path counters
+constexpr size_t kNaError = 64;        // error flag
+constexpr size_t kNaRecs = 128;        // kMaxRecorders DevRecorder
+constexpr size_t kNaVis = kNaRecs + sizeof(DevRecorder) * kMaxRecorders;
+constexpr size_t kNaFirstLast = 2048;  // kMaxTracks x 3 int2
+static_assert(kNaVis + sizeof(int) * kMaxRecorders <= kNaFirstLast, "no-alloc scratch layout");
+static_assert(kNaFirstLast + sizeof(int2) * 3 * kMaxTracks <= (size_t)kNoAllocScratchBytes,
+              "no-alloc scratch layout");
+
+// Shared by every call on a device; holds the last call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on `device` (which must be current).
+// The first call per device resolves it with cudaGetSymbolAddress.
+ear_status noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return fail(EAR_ERR_INVALID_ARG, "device ordinal %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(EAR_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[device] = static_cast<unsigned char*>(ptr);
+  }
+  *out = g_noalloc_ptr[device];
+  return EAR_OK;
+}
+
+}  // namespace
+
+extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
+                                         const ear_recorder* recs, int32_t nrec,
+                                         const ear_render_params* p, float* hist,
+                                         int32_t* first_sample, int32_t* last_sample,
+                                         ear_render_stats* stats) {
+  g_err[0] = 0;
+  if (!s || !src || !p || !hist || (nrec > 0 && !recs))
+    return fail(EAR_ERR_INVALID_ARG, "null argument");
+  if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
+  if (nrec < 0 || nrec > kMaxRecorders)
+    return fail(EAR_ERR_INVALID_ARG,
+                "ear_render_noalloc: %d recorders exceed its fixed scratch (at most %d)", nrec,
+                kMaxRecorders);
+  if (src->num_emitter_triangles != 0)
+    return fail(EAR_ERR_UNSUPPORTED,
+                "ear_render_noalloc: area emitters need per-call scratch; use ear_render");
+  if (p->num_bins <= 0 || p->num_bins > (1 << 30) || (p->num_bins & 3))
+    return fail(EAR_ERR_INVALID_ARG,
+                "ear_render_noalloc: num_bins must be a positive multiple of 4 (got %d)",
+                p->num_bins);
+  if (((uintptr_t)hist) & 15)
+    return fail(EAR_ERR_INVALID_ARG, "ear_render_noalloc: hist must be 16-byte aligned");
+  if (p->bands_mask == 0 || (p->bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
+  if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
+  if (p->num_rays > (1ull << 47)) return fail(EAR_ERR_INVALID_ARG, "num_rays above 2^47");
+  DevRecorder dr[kMaxRecorders];
+  int tracks = 0;
+  for (int i = 0; i < nrec; ++i) {
+    const ear_recorder& r = recs[i];
+    if (r.channels != 1 && r.channels != 2)
+      return fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
+    DevRecorder& d = dr[i];
+    for (int k = 0; k < 3; ++k) {
+      d.loc[k] = r.location[k];
+      d.right[k] = r.right_ear[k];
+      const float h = powf_portable(1.0f - r.head_absorption[k], 4.0f);
+      d.habs[k] = (0.0f < h) ? h : 0.0f;
+    }
+    d.head_size = r.head_size;
+    d.channels = r.channels;
+    d.track0 = tracks;
+    tracks += r.channels;
+  }
+  CU(cudaSetDevice(s->device));
+  unsigned char* scratch = nullptr;
+  ear_status rc = noalloc_scratch(s->device, &scratch);
+  if (rc != EAR_OK) return rc;
+
+  TraceArgs a;
+  std::memset(&a, 0, sizeof a);
+  const TraceOps* ops = (p->flags & EAR_FLAG_EXACT) ? &kTraceExact : &kTraceFast;
+  a.nodes = s->ds.nodes;
+  a.tris = s->ds.tris;
+  a.nrm = s->ds.nrm;
+  a.num_tris = (int)s->ds.num_tris;
+  a.num_nodes = (int)s->ds.num_nodes;
+  a.mats = s->mats;
+  a.num_mats = s->num_mats;
+  a.num_recs = nrec;
+  DevRecorder* recs_dev = reinterpret_cast<DevRecorder*>(scratch + kNaRecs);
+  a.recs = recs_dev;
+  for (int k = 0; k < 3; ++k) a.src[k] = src->location[k];
+  a.k0 = (uint32_t)p->seed;
+  a.k1 = (uint32_t)(p->seed >> 32);
+  a.context = p->context;
+  int nb = 0;
+  for (int b = 0; b < 3; ++b) {
+    a.bands[b] = -1;
+    if (p->bands_mask & (1u << b)) a.bands[nb++] = b;
+    a.air[b] = 1.0f - p->air_absorption[b];
+  }
+  a.num_rays = p->num_rays;
+  a.num_items = p->num_rays * (uint64_t)nb;
+  a.max_bounces = p->max_bounces;
+  a.cutoff = p->cutoff;
+  a.box_pad = s->ds.box_pad;
+  a.hist = hist;
+  a.stride = p->num_bins;
+  a.num_bins = p->num_bins;
+  a.num_tracks = tracks;
+  a.first_last = reinterpret_cast<int2*>(scratch + kNaFirstLast);
+  const bool direct = !(p->flags & (EAR_FLAG_RAW | EAR_FLAG_NO_DIRECT)) && nrec > 0;
+  a.direct_vis = direct ? reinterpret_cast<int*>(scratch + kNaVis) : nullptr;
+  a.counters = reinterpret_cast<unsigned long long*>(scratch + kNaCounters);
+  a.error_flag = reinterpret_cast<int*>(scratch + kNaError);
+  a.traverse_budget = (int)std::min<int64_t>(4 * s->ds.num_nodes + 64, (int64_t)1 << 30);
+  a.dbg_band = -1;
+
+  cudaStream_t st = (cudaStream_t)p->stream;
+  const int rows = tracks * 3;
+  // the shared scratch keeps the previous call's contents: clear it
+  CU(cudaMemsetAsync(scratch, 0, kNaRecs, st));
+  if (nrec) CU(cudaMemcpyAsync(recs_dev, dr, sizeof(DevRecorder) * nrec, cudaMemcpyHostToDevice, st));
+  if (rows) {
+    CU(cudaMemsetAsync(hist, 0, sizeof(float) * (size_t)rows * (size_t)p->num_bins, st));
+    k_init_first_last<<<(rows + 127) / 128, 128, 0, st>>>(a.first_last, rows);
+    CU(cudaGetLastError());
+  }
+  const size_t smem = sizeof(DevMaterial) * (size_t)s->num_mats + sizeof(int) * 2 * 3 * (size_t)tracks;
+  if (smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
+  int per_sm = 0;
+  CU(ops->occupancy(false, smem, &per_sm));
+  if (per_sm < 1) per_sm = 1;
+  CU(cudaEventRecord(s->ev0, st));
+  CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, smem, false, st));
+  CU(cudaEventRecord(s->ev1, st));
+  if (!(p->flags & EAR_FLAG_RAW) && nrec > 0) {
+    const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
+    FinalizeArgs f;
+    f.hist = hist;
+    f.stride = p->num_bins;
+    f.num_bins = p->num_bins;
+    f.first_last = a.first_last;
+    f.recs = a.recs;
+    f.direct_vis = a.direct_vis;
+    for (int k = 0; k < 3; ++k) {
+      f.src[k] = a.src[k];
+      f.air[k] = a.air[k];
+    }
+    f.dry = p->dry_level;
+    f.inv_amount = 1.0f / amount;
+    f.gain2 = src->gain * src->gain;
+    f.bands = p->bands_mask;
+    k_finalize<<<nrec * 3, 256, 0, st>>>(f);
+    CU(cudaGetLastError());
+  }
+  int2 fl[3 * kMaxTracks];
+  unsigned long long cnt[kNumCounters];
+  int errflag = 0;
+  if (rows) CU(cudaMemcpyAsync(fl, a.first_last, sizeof(int2) * rows, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(cnt, a.counters, sizeof cnt, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(&errflag, a.error_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  if (errflag & kErrIndex)
+    return fail(EAR_ERR_CUDA, "internal: a device-side index check failed (corrupt BVH or scene data)");
+  if (errflag & kErrBudget)
+    return fail(EAR_ERR_DEVICE_BUDGET, "a BVH traversal exceeded its iteration budget");
+  for (int i = 0; i < rows; ++i) {
+    if (first_sample) first_sample[i] = std::min(fl[i].x, p->num_bins);
+    if (last_sample) last_sample[i] = std::min(fl[i].y, p->num_bins);
+  }
+  if (stats) {
+    float ms = 0.0f;
+    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    stats->rays = std::min<unsigned long long>(cnt[kWork], a.num_items);
+    stats->segments = cnt[kSegments];
+    stats->shadow_queries = cnt[kShadow];
+    stats->contributions = cnt[kContrib];
+    stats->sampler_overflows = cnt[kOverflow];
+    stats->node_visits = cnt[kNodeVisits];
+    stats->triangle_tests = cnt[kTriTests];
+    stats->splat_bins = cnt[kSplatBins];
+    stats->kernel_ms = ms;
+  }
+  return EAR_OK;
+}

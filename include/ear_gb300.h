@@ -206,6 +206,37 @@ ear_status ear_trace_debug(ear_scene* scene, const ear_source* source,
                            int32_t max_record, int32_t* hit_tri,
                            uint8_t* bounce_type, uint32_t* visible);
 
+/* ear_render without any allocation.  No counterpart in the reference.
+   For callers that must not allocate while rendering: an audio engine that
+   re-renders an impulse response from its real-time thread when a listener
+   moves cannot take the unbounded latency and device-wide synchronisation
+   of cudaMalloc / cudaFree, and a host that runs the tracer inside a fixed
+   GPU memory budget cannot let the library grow its own buffers.  The scene
+   handle (created beforehand) and `hist` are the caller's; every other
+   buffer the render needs lives in one statically sized device array
+   (16 KiB: the recorder table, counters and per-track bookkeeping), so the
+   call makes no cudaMalloc, cudaFree or host heap allocation.
+   - hist: DEVICE pointer, 16-byte aligned, float[num_tracks][3][num_bins];
+     it is zeroed and accumulated in place.  num_bins must be a multiple
+     of 4.  first_sample / last_sample / stats are optional HOST pointers
+     laid out as in ear_histograms / ear_render_stats.
+   - Limits: at most 32 recorders (64 tracks); point sources only (an area
+     emitter needs per-call scratch: EAR_ERR_UNSUPPORTED).  Larger requests
+     are rejected with EAR_ERR_INVALID_ARG and a message.
+   - The first call on a device resolves the array's device address
+     (cudaGetSymbolAddress) with that device current; make that first call
+     before any stream capture.
+   - The array is shared by every call on the device and keeps the last
+     call's contents (each call clears what must start at zero).  Calls
+     whose GPU work overlaps -- e.g. on two streams -- race on it: serialise
+     them. */
+ear_status ear_render_noalloc(ear_scene* scene, const ear_source* source,
+                              const ear_recorder* recorders,
+                              int32_t num_recorders,
+                              const ear_render_params* params, float* hist,
+                              int32_t* first_sample, int32_t* last_sample,
+                              ear_render_stats* stats);
+
 /* --------------------------------------- host post-processing (FloatBuffer)
  * Mirrors of FloatBuffer / RecorderTrack (src/Recorder.cpp:33-118, 303-340)
  * on one track.  `first`/`last` are the bookkeeping values above; the track
