@@ -231,6 +231,57 @@ def _config(w, args, flush):
             "l2": flush}
 
 
+def adjoint_ratio(device: int, rays: int, steps: int):
+    """Time of the path-replay adjoint (ear_render_adjoint, upstream gradient
+    resident on the device) over the time of the forward render it
+    differentiates (ear_render, exact kernels, histograms to the device), on
+    the 8-material inverse-problem shoebox, CUDA events on the same stream."""
+    import torch
+
+    from ear_gb300 import Tracer, scenes
+
+    w, _, _ = scenes.inverse_shoebox(num_rays=rays)
+    kw = dict(w.render, exact=True)
+    dev = torch.device("cuda", device)
+    stream = torch.cuda.current_stream(dev)
+    out = torch.zeros((w.num_tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
+    g = torch.randn((w.num_tracks, 3, kw["num_bins"]), generator=torch.Generator().manual_seed(0))
+    g = g.to(dev)
+    with Tracer(w.vertices, w.material_ids, w.materials, device=device) as tr:
+        fwd = tr.render(w.source, w.recorders, out=out, **kw)
+        book = dict(first=fwd.first_sample, last=fwd.last_sample)
+
+        def run(which):
+            if which == "fwd":
+                r = tr.render(w.source, w.recorders, out=out, **kw)
+                return r.stats
+            # the raw bookkeeping comes from a host render of the same rays
+            return tr.render_adjoint(w.source, w.recorders, g, raw_first=rf, raw_last=rl, **book,
+                                     **kw)[1]
+
+        host = tr.render(w.source, w.recorders, **kw)
+        rf, rl = host.raw_first_sample, host.raw_last_sample
+        res = {}
+        for which in ("fwd", "adj"):
+            for _ in range(3):
+                run(which)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            seg = 0
+            for _ in range(steps):
+                seg += int(run(which)["segments"])
+            e1.record(stream)
+            e1.synchronize()
+            res[which] = (e0.elapsed_time(e1) / steps, seg // steps)
+    return {"workload": w.name, "rays_per_band": rays, "materials": len(w.materials),
+            "forward_ms": res["fwd"][0], "adjoint_ms": res["adj"][0],
+            "ratio": res["adj"][0] / res["fwd"][0], "segments_per_pass": res["fwd"][1],
+            "adjoint_segments_per_pass": res["adj"][1],
+            "path": "ear_render (exact) vs ear_render_adjoint (exact, d_hist on device)"}
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -281,8 +332,8 @@ def run_ours(args):
         kern_ms += res.stats["kernel_ms"]
         for k in agg:
             agg[k] += int(res.stats[k])
-        # per step: trace kernel + 2 scale passes + direct-sound kernel + first/last init
-        launches += 5
+        # per step: first/last init, the persistent trace kernel, finalize
+        launches += 3
     torch.cuda.synchronize()
     barrier(world)
     wall = time.perf_counter() - t_wall
@@ -327,6 +378,10 @@ def run_ours(args):
                "path": "ear_scene_create (pinned host) + ear_scene_build_bvh + ear_render "
                        "(histograms to pinned host) + ear_scene_destroy"}
 
+    adj = None
+    if not args.no_adjoint:
+        adj = adjoint_ratio(local, args.adjoint_rays, max(1, min(args.steps, 5)))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(w, args.cpu_rays or _default_cpu_rays(args.workload), os.cpu_count() or 1)
@@ -349,6 +404,7 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": per_launch,
                          "kernel_ms_per_launch": kern_ms / args.steps},
             "e2e": e2e,
+            "adjoint": adj,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clk,
@@ -372,6 +428,8 @@ def main():
     ap.add_argument("--box-pad", type=float, default=-1.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-rays", type=int, default=1_000_000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

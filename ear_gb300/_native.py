@@ -75,7 +75,8 @@ class EarRenderStats(C.Structure):
 
 class EarHistograms(C.Structure):
     _fields_ = [("data", C.c_void_p), ("first_sample", C.c_void_p), ("last_sample", C.c_void_p),
-                ("on_device", C.c_int32), ("reserved0", C.c_int32)]
+                ("on_device", C.c_int32), ("reserved0", C.c_int32),
+                ("raw_first_sample", C.c_void_p), ("raw_last_sample", C.c_void_p)]
 
 
 # Every exported symbol of include/ear_gb300.h with its ctypes signature.
@@ -95,6 +96,11 @@ SIGNATURES = {
     "ear_trace_debug": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
                                   C.c_int32, C.POINTER(EarRenderParams), C.c_int32, C.c_int32,
                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ear_scene_set_materials": (C.c_int, [C.c_void_p, C.POINTER(EarMaterial), C.c_int32]),
+    "ear_render_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
+                                     C.c_int32, C.POINTER(EarRenderParams), C.c_void_p, C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(EarRenderStats)]),
     "ear_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
                                      C.c_int32, C.POINTER(EarRenderParams), C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.POINTER(EarRenderStats)]),

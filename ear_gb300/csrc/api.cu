@@ -21,6 +21,17 @@
 #include "ear_internal.h"
 #include "ear_record.cuh"
 
+namespace ear {
+size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block) {
+  size_t b = sizeof(DevMaterial) * (size_t)num_mats + sizeof(int) * 6 * (size_t)num_tracks;
+  if (mode == kModeAdjoint) {
+    b = (b + 7) & ~(size_t)7;
+    b += sizeof(double) * 6 * (size_t)num_mats + sizeof(float) * 2 * (size_t)num_mats * (size_t)block;
+  }
+  return b;
+}
+}  // namespace ear
+
 using namespace ear;
 
 namespace {
@@ -58,6 +69,8 @@ bool derive_material(const ear_material& m, DevMaterial* o) {
     if ((double)fl < 0.0001 && (double)fr < 0.0001) o->always_reflect |= 1u << i;
     o->p_reflect[i] = fl / (fl + fr);
     o->spec[i] = m.has_specularity ? m.specularity[i] : 0.0f;
+    o->refl[i] = fl;
+    o->refr[i] = fr;
   }
   return true;
 }
@@ -302,7 +315,8 @@ struct Prepared {
 };
 
 ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs, int32_t nrec,
-                   const ear_render_params* p, uint32_t bands_mask, Prepared* out) {
+                   const ear_render_params* p, uint32_t bands_mask, Prepared* out,
+                   int mode = kModeForward) {
   if (!s || !src || !p || (nrec > 0 && !recs)) return fail(EAR_ERR_INVALID_ARG, "null argument");
   if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
   if (nrec < 0 || nrec > kMaxRecorders)
@@ -377,7 +391,7 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   a.hist = s->hist;
   a.first_last = s->fl;
   const bool direct = !(p->flags & (EAR_FLAG_RAW | EAR_FLAG_NO_DIRECT)) &&
-                      src->num_emitter_triangles <= 0 && nrec > 0;
+                      src->num_emitter_triangles <= 0 && nrec > 0 && mode != kModeAdjoint;
   a.direct_vis = direct ? s->dvis : nullptr;
   a.counters = s->counters;
   a.error_flag = s->err;
@@ -414,10 +428,10 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
     k_init_first_last<<<(tracks * 3 + 127) / 128, 128, 0, st>>>(s->fl, tracks * 3);
     CU(cudaGetLastError());
   }
-  out->smem = sizeof(DevMaterial) * (size_t)s->num_mats + sizeof(int) * 2 * 3 * (size_t)tracks;
+  out->smem = trace_smem_bytes(s->num_mats, tracks, mode, out->ops->block);
   if (out->smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
   int per_sm = 0;
-  CU(out->ops->occupancy(false, out->smem, &per_sm));
+  CU(out->ops->occupancy(mode, out->smem, &per_sm));
   if (per_sm < 1) per_sm = 1;
   out->grid = s->sm_count * per_sm;
   return EAR_OK;
@@ -455,9 +469,13 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
   cudaStream_t st = (cudaStream_t)p->stream;
   CU(cudaEventRecord(s->ev0, st));
   // with no rays the launch still computes the direct-sound visibility
-  CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.smem, false, st));
+  CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.smem, kModeForward, st));
   CU(cudaEventRecord(s->ev1, st));
   const int rows = pr.num_tracks * 3;
+  std::vector<int2> fl_raw((size_t)std::max(rows, 1));
+  const bool want_raw = rows > 0 && (out->raw_first_sample || out->raw_last_sample);
+  if (want_raw)
+    CU(cudaMemcpyAsync(fl_raw.data(), a.first_last, sizeof(int2) * rows, cudaMemcpyDeviceToHost, st));
   if (!(p->flags & EAR_FLAG_RAW) && nrec > 0) {
     // amount is a float incremented once per ray (src/Scene.cpp:122,127):
     // exact to 2^24 rays, then stuck at 2^24.
@@ -492,15 +510,19 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
   double ms = 0.0;
   rc = finish(s, p, pr, &ms);
   if (rc != EAR_OK) return rc;
-  if (out->first_sample || out->last_sample) {
-    std::vector<int32_t> f((size_t)std::max(rows, 1)), l((size_t)std::max(rows, 1));
+  const cudaMemcpyKind k2 = out->on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<int2>& src_fl = pass == 0 ? fl : fl_raw;
+    int32_t* dst_f = pass == 0 ? out->first_sample : out->raw_first_sample;
+    int32_t* dst_l = pass == 0 ? out->last_sample : out->raw_last_sample;
+    if ((!dst_f && !dst_l) || rows == 0) continue;
+    std::vector<int32_t> f((size_t)rows), l((size_t)rows);
     for (int i = 0; i < rows; ++i) {
-      f[(size_t)i] = std::min(fl[(size_t)i].x, a.num_bins);
-      l[(size_t)i] = std::min(fl[(size_t)i].y, a.num_bins);
+      f[(size_t)i] = std::min(src_fl[(size_t)i].x, a.num_bins);
+      l[(size_t)i] = std::min(src_fl[(size_t)i].y, a.num_bins);
     }
-    const cudaMemcpyKind k2 = out->on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
-    if (out->first_sample && rows) CU(cudaMemcpy(out->first_sample, f.data(), sizeof(int32_t) * rows, k2));
-    if (out->last_sample && rows) CU(cudaMemcpy(out->last_sample, l.data(), sizeof(int32_t) * rows, k2));
+    if (dst_f) CU(cudaMemcpy(dst_f, f.data(), sizeof(int32_t) * rows, k2));
+    if (dst_l) CU(cudaMemcpy(dst_l, l.data(), sizeof(int32_t) * rows, k2));
   }
   if (stats) {
     stats->rays = std::min<unsigned long long>(cnt[kWork], a.num_items);
@@ -524,7 +546,7 @@ extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
   if (!p || !hit_tri || !bounce_type || !visible || max_record <= 0 || band < 0 || band > 2)
     return fail(EAR_ERR_INVALID_ARG, "bad debug arguments");
   Prepared pr;
-  ear_status rc = prepare(s, src, recs, nrec, p, 1u << band, &pr);
+  ear_status rc = prepare(s, src, recs, nrec, p, 1u << band, &pr, kModeDebug);
   if (rc != EAR_OK) return rc;
   TraceArgs& a = pr.a;
   const size_t n = (size_t)p->num_rays * (size_t)max_record;
@@ -548,7 +570,7 @@ extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
     a.dbg_bt = db;
     a.dbg_vis = dv;
     e = cudaEventRecord(s->ev0, st);
-    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, true, st);
+    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, kModeDebug, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(hit_tri, dh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(bounce_type, db, n, cudaMemcpyDeviceToHost, st);
@@ -560,6 +582,131 @@ extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
   cudaFree(dv);
   if (e != cudaSuccess) return fail(EAR_ERR_CUDA, "debug trace: %s", cudaGetErrorString(e));
   return finish(s, p, pr, nullptr);
+}
+
+// ---------------------------------------------------------- materials
+extern "C" ear_status ear_scene_set_materials(ear_scene* s, const ear_material* materials,
+                                              int32_t num_materials) {
+  g_err[0] = 0;
+  if (!s || (num_materials > 0 && !materials)) return fail(EAR_ERR_INVALID_ARG, "null argument");
+  if (num_materials != s->num_mats)
+    return fail(EAR_ERR_INVALID_ARG, "expected %d materials, got %d", s->num_mats, num_materials);
+  std::vector<DevMaterial> mats((size_t)num_materials);
+  for (int i = 0; i < num_materials; ++i)
+    if (!derive_material(materials[i], &mats[(size_t)i]))
+      return fail(EAR_ERR_INVALID_ARG, "Invalid material settings (material %d)", i);
+  CU(cudaSetDevice(s->device));
+  if (num_materials)
+    CU(cudaMemcpy(s->mats, mats.data(), sizeof(DevMaterial) * mats.size(), cudaMemcpyHostToDevice));
+  return EAR_OK;
+}
+
+// ------------------------------------------------------------- adjoint
+namespace {
+
+// Upstream gradient of the finalized histogram -> gradient of the raw splat
+// sums: bins scaled by 1/N inside the pre-direct [first, real_length) and
+// by gain^2 inside the final one (src/Scene.cpp:291,314).
+__global__ void k_adjoint_scale(const float* g, int g_pitch, float* out, int stride, int nb,
+                                int rows, const int4* ranges, float inv_amount, float gain2,
+                                int scaled) {
+  const int row = blockIdx.y;
+  if (row >= rows) return;
+  const int4 r = ranges[row];  // raw first, raw last, final first, final last
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < stride; i += gridDim.x * blockDim.x) {
+    float v = 0.0f;
+    if (i < nb) {
+      v = g[(size_t)row * g_pitch + i];
+      if (scaled) {
+        if (i >= r.x && i < r.y) v *= inv_amount;
+        if (i >= r.z && i < r.w) v *= gain2;
+      }
+    }
+    out[(size_t)row * stride + i] = v;
+  }
+}
+
+}  // namespace
+
+extern "C" ear_status ear_render_adjoint(ear_scene* s, const ear_source* src,
+                                         const ear_recorder* recs, int32_t nrec,
+                                         const ear_render_params* p, const float* d_hist,
+                                         int32_t d_hist_on_device, const int32_t* raw_first,
+                                         const int32_t* raw_last, const int32_t* first,
+                                         const int32_t* last, double* grad,
+                                         ear_render_stats* stats) {
+  g_err[0] = 0;
+  if (!p || !d_hist || !grad) return fail(EAR_ERR_INVALID_ARG, "null argument");
+  const bool scaled = !(p->flags & EAR_FLAG_RAW);
+  if (scaled && (!raw_first || !raw_last || !first || !last))
+    return fail(EAR_ERR_INVALID_ARG, "the bookkeeping of the forward render is required");
+  if (s && s->num_mats > 32) return fail(EAR_ERR_UNSUPPORTED, "the adjoint supports at most 32 materials");
+  Prepared pr;
+  ear_status rc = prepare(s, src, recs, nrec, p, p->bands_mask, &pr, kModeAdjoint);
+  if (rc != EAR_OK) return rc;
+  TraceArgs& a = pr.a;
+  cudaStream_t st = (cudaStream_t)p->stream;
+  const int rows = pr.num_tracks * 3;
+  // scaled upstream gradient in the (otherwise idle) histogram scratch
+  float* g_in = nullptr;
+  int4* ranges = nullptr;
+  double* dgrad = nullptr;
+  const size_t ngrad = (size_t)s->num_mats * 6;
+  cudaError_t e = cudaSuccess;
+  std::vector<int4> hr((size_t)std::max(rows, 1));
+  for (int i = 0; i < rows; ++i)
+    hr[(size_t)i] = scaled ? make_int4(raw_first[i], raw_last[i], first[i], last[i]) : make_int4(0, 0, 0, 0);
+  if (rows) {
+    if (!d_hist_on_device) {
+      e = cudaMalloc(&g_in, sizeof(float) * (size_t)rows * a.num_bins);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g_in, d_hist, sizeof(float) * (size_t)rows * a.num_bins,
+                            cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&ranges, sizeof(int4) * rows);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ranges, hr.data(), sizeof(int4) * rows, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&dgrad, sizeof(double) * std::max<size_t>(ngrad, 1));
+  if (e == cudaSuccess) e = cudaMemsetAsync(dgrad, 0, sizeof(double) * std::max<size_t>(ngrad, 1), st);
+  if (e == cudaSuccess && rows) {
+    const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
+    const dim3 grid((unsigned)std::min(1024, (a.stride + 255) / 256), (unsigned)rows);
+    k_adjoint_scale<<<grid, 256, 0, st>>>(d_hist_on_device ? d_hist : g_in, a.num_bins, a.hist,
+                                          a.stride, a.num_bins, rows, ranges, 1.0f / amount,
+                                          src->gain * src->gain, scaled ? 1 : 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    a.adj_g = a.hist;
+    a.adj_grad = dgrad;
+    e = cudaEventRecord(s->ev0, st);
+    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, kModeAdjoint, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
+  }
+  unsigned long long cnt[kNumCounters] = {0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(grad, dgrad, sizeof(double) * ngrad, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, a.counters, sizeof cnt, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(g_in);
+  cudaFree(ranges);
+  cudaFree(dgrad);
+  if (e != cudaSuccess) return fail(EAR_ERR_CUDA, "adjoint: %s", cudaGetErrorString(e));
+  double ms = 0.0;
+  rc = finish(s, p, pr, &ms);
+  if (rc != EAR_OK) return rc;
+  if (stats) {
+    stats->rays = std::min<unsigned long long>(cnt[kWork], a.num_items);
+    stats->segments = cnt[kSegments];
+    stats->shadow_queries = cnt[kShadow];
+    stats->contributions = cnt[kContrib];
+    stats->sampler_overflows = cnt[kOverflow];
+    stats->node_visits = cnt[kNodeVisits];
+    stats->triangle_tests = cnt[kTriTests];
+    stats->splat_bins = cnt[kSplatBins];
+    stats->kernel_ms = ms;
+  }
+  return EAR_OK;
 }
 
 // ------------------------------------------------- FloatBuffer post-process
@@ -807,13 +954,13 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     k_init_first_last<<<(rows + 127) / 128, 128, 0, st>>>(a.first_last, rows);
     CU(cudaGetLastError());
   }
-  const size_t smem = sizeof(DevMaterial) * (size_t)s->num_mats + sizeof(int) * 2 * 3 * (size_t)tracks;
+  const size_t smem = trace_smem_bytes(s->num_mats, tracks, kModeForward, ops->block);
   if (smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
   int per_sm = 0;
-  CU(ops->occupancy(false, smem, &per_sm));
+  CU(ops->occupancy(kModeForward, smem, &per_sm));
   if (per_sm < 1) per_sm = 1;
   CU(cudaEventRecord(s->ev0, st));
-  CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, smem, false, st));
+  CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, smem, kModeForward, st));
   CU(cudaEventRecord(s->ev1, st));
   if (!(p->flags & EAR_FLAG_RAW) && nrec > 0) {
     const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;

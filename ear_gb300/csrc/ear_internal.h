@@ -48,6 +48,8 @@ struct DevMaterial {
   float p_reflect[3];
   float spec[3];
   uint32_t always_reflect;
+  float refl[3];  // the MAT values, for the adjoint's score terms
+  float refr[3];  // (0 when opaque)
 };
 
 struct DevRecorder {
@@ -92,6 +94,10 @@ struct TraceArgs {
   int num_tracks;
   int2* first_last;  // [track][band]
   int* direct_vis;   // [recorder] direct-path visibility, or null
+  // adjoint mode: upstream gradient of the raw splat sums [track][band][stride]
+  // and the gradient accumulators [material][band][2 = absorption, refraction]
+  const float* adj_g;
+  double* adj_grad;
   unsigned long long* counters;  // [0] work, [1] segments, [2] shadow, [3] contrib, [4] overflow
   int* error_flag;
   int traverse_budget;
@@ -122,11 +128,14 @@ enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char* err, size_t errlen);
 
 // Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
+enum TraceMode { kModeForward = 0, kModeDebug = 1, kModeAdjoint = 2 };
 struct TraceOps {
-  cudaError_t (*trace)(const TraceArgs& a, int grid, size_t smem, bool debug, cudaStream_t s);
-  cudaError_t (*occupancy)(bool debug, size_t smem, int* blocks_per_sm);
+  cudaError_t (*trace)(const TraceArgs& a, int grid, size_t smem, int mode, cudaStream_t s);
+  cudaError_t (*occupancy)(int mode, size_t smem, int* blocks_per_sm);
   int block;
 };
+// Dynamic shared memory of a trace launch.
+size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block);
 extern const TraceOps kTraceExact;
 extern const TraceOps kTraceFast;
 

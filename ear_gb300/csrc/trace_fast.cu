@@ -6,30 +6,32 @@
 namespace ear {
 namespace {
 
-cudaError_t trace_fast(const TraceArgs& a, int grid, size_t smem, bool debug, cudaStream_t s) {
-  if (debug) {
-    cudaFuncSetAttribute(fast::trace_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    fast::trace_kernel<true><<<grid, fast::kTraceBlock, smem, s>>>(a);
-  } else {
-    cudaFuncSetAttribute(fast::trace_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    fast::trace_kernel<false><<<grid, fast::kTraceBlock, smem, s>>>(a);
-  }
+template <int MODE>
+cudaError_t launch(const TraceArgs& a, int grid, size_t smem, cudaStream_t s) {
+  cudaFuncSetAttribute(fast::trace_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  fast::trace_kernel<MODE><<<grid, fast::kTraceBlock, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t occupancy_fast(bool debug, size_t smem, int* blocks_per_sm) {
-  if (debug) {
-    cudaFuncSetAttribute(fast::trace_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fast::trace_kernel<true>,
-                                                         fast::kTraceBlock, smem);
-  }
-  cudaFuncSetAttribute(fast::trace_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int MODE>
+cudaError_t occupancy(size_t smem, int* blocks_per_sm) {
+  cudaFuncSetAttribute(fast::trace_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fast::trace_kernel<false>,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fast::trace_kernel<MODE>,
                                                        fast::kTraceBlock, smem);
+}
+
+cudaError_t trace_fast(const TraceArgs& a, int grid, size_t smem, int mode, cudaStream_t s) {
+  if (mode == kModeDebug) return launch<kModeDebug>(a, grid, smem, s);
+  if (mode == kModeAdjoint) return launch<kModeAdjoint>(a, grid, smem, s);
+  return launch<kModeForward>(a, grid, smem, s);
+}
+
+cudaError_t occupancy_fast(int mode, size_t smem, int* blocks_per_sm) {
+  if (mode == kModeDebug) return occupancy<kModeDebug>(smem, blocks_per_sm);
+  if (mode == kModeAdjoint) return occupancy<kModeAdjoint>(smem, blocks_per_sm);
+  return occupancy<kModeForward>(smem, blocks_per_sm);
 }
 
 }  // namespace

@@ -287,15 +287,39 @@ __device__ __forceinline__ void splat(float* row, int* first, int* last, int nb,
   if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(row + 4 * grp), acc);
 }
 
-__device__ __forceinline__ void record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir,
-                                       float amp, float t, float dist, int* s_first, int* s_last,
-                                       uint32_t& bins) {
+// Adjoint counterpart of splat(): the dot product of the upstream gradient
+// with the splat values, over the same positions.
+__device__ __forceinline__ float gather(const float* __restrict__ g, int nb, long long s, int w,
+                                        float ampl, float step) {
+  float v = ampl, acc = 0.0f;
+  for (int i = 0; i < w; ++i) {
+    const long long pos = s + i;
+    if (pos >= nb) break;
+    if (pos >= 0) acc += __ldg(g + pos) * v;
+    v -= step;
+  }
+  return acc;
+}
+
+// Records one contribution (forward) or returns its gradient weight
+// sum_i g[s+i] * v_i (adjoint).
+template <int MODE>
+__device__ __forceinline__ float record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir,
+                                        float amp, float t, float dist, int* s_first, int* s_last,
+                                        uint32_t& bins) {
   const SplatPlan p = record_plan(R, band, dir, amp, t, dist);
+  float G = 0.0f;
   for (int k = 0; k < p.tracks; ++k) {
     const int tb = (R.track0 + k) * 3 + band;
-    splat(a.hist + (size_t)tb * (size_t)a.stride, s_first + tb, s_last + tb, a.num_bins, p.s[k],
-          p.w, p.ampl[k], p.step[k], bins);
+    if (MODE == kModeAdjoint) {
+      G += gather(a.adj_g + (size_t)tb * (size_t)a.stride, a.num_bins, p.s[k], p.w, p.ampl[k],
+                  p.step[k]);
+    } else {
+      splat(a.hist + (size_t)tb * (size_t)a.stride, s_first + tb, s_last + tb, a.num_bins, p.s[k],
+            p.w, p.ampl[k], p.step[k], bins);
+    }
   }
+  return G;
 }
 
 // --------------------------------------------------------------- paths
@@ -305,6 +329,16 @@ struct PathState {
   int k;
   int band;
   uint64_t ray;
+  float P, T;  // adjoint: gradient weights of the contributions so far / in total
+};
+
+// Adjoint bookkeeping in shared memory: per thread, the per-material sums
+// A[m] of v_j = grad log(weight of the choice at bounce j) -- the weight of
+// a REFLECT is refl, of a REFRACT refr (survival times choice probability);
+// per block, the gradient accumulators [material][band][2].
+struct AdjShared {
+  float* A;       // this thread's A[num_mats][2]
+  double* grad;   // block accumulators
 };
 
 // The state a vertex hands to the recorder phase.
@@ -318,9 +352,10 @@ struct Vertex {
 
 // Visibility + contribution of recorder `ri` at the current vertex
 // (src/Scene.cpp:188-268).  Returns whether the recorder is visible.
-__device__ __forceinline__ bool connect_one(const TraceArgs& a, const PathState& st,
-                                            const Vertex& vx, int ri, LaneCounters& c, int& err,
-                                            int* s_first, int* s_last) {
+template <int MODE>
+__device__ __forceinline__ bool connect_one(const TraceArgs& a, PathState& st, const Vertex& vx,
+                                            int ri, LaneCounters& c, int& err, int* s_first,
+                                            int* s_last) {
   const DevRecorder& R = a.recs[ri];
   const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
   c.shadow++;
@@ -358,15 +393,20 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const PathState&
     if (k & 1) I *= -1.0f;
     c.contrib++;
     const float total = st.L + len;
-    record(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last, c.bins);
+    const float G = record<MODE>(a, R, st.band, lsdir, I, total / 343.0f, total, s_first, s_last,
+                                 c.bins);
+    if (MODE == kModeAdjoint) {
+      st.P += G;
+      st.T += G;
+    }
   }
   return true;
 }
 
-template <bool DEBUG>
+template <int MODE>
 __device__ __forceinline__ void debug_put(const TraceArgs& a, const PathState& st, int k, int hit,
                                           int bt, uint32_t vis, int what) {
-  if (!DEBUG) return;
+  if (MODE != kModeDebug) return;
   if (st.band != a.dbg_band || (int64_t)st.ray >= a.dbg_rays || k < 1 || k > a.dbg_max_record)
     return;
   const size_t i = (size_t)st.ray * a.dbg_max_record + (k - 1);
@@ -377,10 +417,17 @@ __device__ __forceinline__ void debug_put(const TraceArgs& a, const PathState& s
 
 // Bounce 0: AbstractSoundFile::SoundRay (src/SoundFile.cpp:215-228).  Area
 // emitters connect the recorders at bounce 0 (src/Scene.cpp:185).
-__device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, Vertex& vx) {
+template <int MODE>
+__device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, Vertex& vx,
+                            const AdjShared& adj) {
   st.I = 1.0f;
   st.L = 0.0f;
   st.k = 0;
+  if (MODE == kModeAdjoint) {
+    st.P = 0.0f;
+    st.T = 0.0f;
+    for (int m = 0; m < 2 * a.num_mats; ++m) adj.A[m] = 0.0f;
+  }
   const uint32_t band = (uint32_t)st.band;
   const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, 0, 0);
   if (a.num_emitter > 0) {
@@ -419,27 +466,53 @@ __device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, 
 // Reflection k = st.k + 1 up to the recorder connections
 // (src/Scene.cpp:150-177): closest hit, Material::Bounce, Sample_Hemi,
 // air and surface losses.  Returns whether the path continues.
-template <bool DEBUG>
+template <int MODE>
 __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict__ mats,
-                              PathState& st, LaneCounters& c, int& err, Vertex& vx) {
+                              PathState& st, LaneCounters& c, int& err, Vertex& vx,
+                              const AdjShared& adj) {
   const int k = st.k + 1;
   const uint32_t band = (uint32_t)st.band;
   c.segments++;
   Hit h;
   traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, c, err);
-  debug_put<DEBUG>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
+  debug_put<MODE>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
   const float4 nm = __ldg(a.nrm + h.pos);
   const float t = h.t;
   const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
   const V3 N = mk(nm.x, nm.y, nm.z);
   V3 n = (dot(N, st.d) > 0.0f) ? neg(N) : N;
-  const DevMaterial& M = mats[clamp_index(__float_as_int(nm.w), a.num_mats, err)];
+  const int mid = clamp_index(__float_as_int(nm.w), a.num_mats, err);
+  const DevMaterial& M = mats[mid];
   // Material::Bounce (src/Material.cpp:76-83)
   const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, (uint32_t)k, 0);
   int bt = 0;
   if (!((M.always_reflect >> band) & 1u)) bt = (uniform24(b0.w) <= M.p_reflect[band]) ? 0 : 1;
-  debug_put<DEBUG>(a, st, k, 0, bt, 0, 1);
+  debug_put<MODE>(a, st, k, 0, bt, 0, 1);
+  if (MODE == kModeAdjoint) {
+    // v = grad log(s P(choice)) w.r.t. (absorption, refraction), with
+    // refl = 1 - absorption - refraction: -1/s from the survival plus the
+    // score of the choice; the sum is -1/refl (REFLECT) or (0, 1/refr)
+    // (REFRACT), and -1/s alone when the choice is forced.
+    float va, vr;
+    if ((M.always_reflect >> band) & 1u) {
+      va = -1.0f / M.survival[band];
+      vr = 0.0f;
+    } else if (bt == 0) {
+      va = -1.0f / M.survival[band] - M.refr[band] / ((M.refl[band] + M.refr[band]) * M.refl[band]);
+      vr = -1.0f / M.refl[band];
+    } else {
+      va = -1.0f / M.survival[band] + 1.0f / (M.refl[band] + M.refr[band]);
+      vr = 1.0f / M.refr[band];
+    }
+    adj.A[2 * mid] += va;
+    adj.A[2 * mid + 1] += vr;
+    if (st.P != 0.0f) {
+      double* gm = adj.grad + ((size_t)mid * 3 + band) * 2;
+      atomicAdd(gm, -(double)va * (double)st.P);
+      atomicAdd(gm + 1, -(double)vr * (double)st.P);
+    }
+  }
   const float spec = M.spec[band];
   V3 base;
   if (bt == 1) {
@@ -467,6 +540,19 @@ __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict_
   return !invalid_float(st.I);
 }
 
+// End of an adjoint path: grad[m][band] += T * A[m].
+__device__ __forceinline__ void adjoint_flush(const TraceArgs& a, const PathState& st,
+                                              const AdjShared& adj) {
+  if (st.T == 0.0f) return;
+  for (int m = 0; m < a.num_mats; ++m) {
+    const float va = adj.A[2 * m], vr = adj.A[2 * m + 1];
+    if (va == 0.0f && vr == 0.0f) continue;
+    double* gm = adj.grad + ((size_t)m * 3 + st.band) * 2;
+    atomicAdd(gm, (double)st.T * (double)va);
+    atomicAdd(gm + 1, (double)st.T * (double)vr);
+  }
+}
+
 // Direct-sound visibility (src/Scene.cpp:299-304): Connect(listener,
 // source) for every recorder, computed by the first threads of block 0
 // with the same any-hit traversal as the path connections.  The lobe
@@ -485,12 +571,21 @@ __device__ void direct_visibility(const TraceArgs& a, int& err) {
   a.direct_vis[r] = blocked ? 0 : 1;
 }
 
-template <bool DEBUG>
+template <int MODE>
 __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevMaterial* s_mats = reinterpret_cast<DevMaterial*>(smem_raw);
   int* s_first = reinterpret_cast<int*>(smem_raw + sizeof(DevMaterial) * a.num_mats);
   int* s_last = s_first + a.num_tracks * 3;
+  AdjShared adj = {nullptr, nullptr};
+  if (MODE == kModeAdjoint) {
+    size_t off = sizeof(DevMaterial) * a.num_mats + sizeof(int) * 6 * a.num_tracks;
+    off = (off + 7) & ~(size_t)7;
+    adj.grad = reinterpret_cast<double*>(smem_raw + off);
+    float* all_A = reinterpret_cast<float*>(adj.grad + 6 * a.num_mats);
+    adj.A = all_A + (size_t)threadIdx.x * 2 * a.num_mats;
+    for (int i = threadIdx.x; i < 6 * a.num_mats; i += blockDim.x) adj.grad[i] = 0.0;
+  }
   {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.mats);
     uint32_t* dst = reinterpret_cast<uint32_t*>(s_mats);
@@ -511,6 +606,8 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
   st.k = 0;
   st.band = 0;
   st.ray = 0;
+  st.P = 0.0f;
+  st.T = 0.0f;
   // Every lane, live or not, passes the same __syncwarp() points below;
   // per-lane work between them is predicated, so divergent loops
   // (traversal, rejection sampling) reconverge at each phase boundary.
@@ -541,24 +638,27 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
     Vertex vx;
     vx.conn = false;
     if (fresh) {
-      emit_vertex(a, st, c, vx);
+      emit_vertex<MODE>(a, st, c, vx, adj);
       alive = true;
     } else if (alive) {
-      alive = bounce_vertex<DEBUG>(a, s_mats, st, c, err, vx);
+      alive = bounce_vertex<MODE>(a, s_mats, st, c, err, vx, adj);
       vx.conn = alive;
+      if (MODE == kModeAdjoint && !alive) adjoint_flush(a, st, adj);
     }
     __syncwarp();
     // phase 3: recorder connections (src/Scene.cpp:185-270)
     uint32_t vis = 0;
     for (int ri = 0; ri < a.num_recs; ++ri) {
-      if (vx.conn && connect_one(a, st, vx, ri, c, err, s_first, s_last)) vis |= 1u << (ri & 31);
+      if (vx.conn && connect_one<MODE>(a, st, vx, ri, c, err, s_first, s_last))
+        vis |= 1u << (ri & 31);
       __syncwarp();
     }
     // phase 4: cut-off, next direction, bounce limit (src/Scene.cpp:275-277)
     if (alive) {
-      if (st.k > 0) debug_put<DEBUG>(a, st, st.k, 0, 0, vis, 2);
+      if (st.k > 0) debug_put<MODE>(a, st, st.k, 0, 0, vis, 2);
       if ((double)st.I < a.cutoff || st.k >= a.max_bounces) {
         alive = false;
+        if (MODE == kModeAdjoint) adjoint_flush(a, st, adj);
       } else {
         st.prev = normalized(st.d);
       }
@@ -587,6 +687,11 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
     }
   }
   __syncthreads();
+  if (MODE == kModeAdjoint) {
+    for (int i = threadIdx.x; i < 6 * a.num_mats; i += blockDim.x)
+      if (adj.grad[i] != 0.0) atomicAdd(a.adj_grad + i, adj.grad[i]);
+    return;
+  }
   for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
     if (s_last[i] > 0) atomicMax(&a.first_last[i].y, s_last[i]);
     if (s_first[i] < kInitialFirstSample) atomicMin(&a.first_last[i].x, s_first[i]);

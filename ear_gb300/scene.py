@@ -138,6 +138,8 @@ class RenderResult:
     first_sample: np.ndarray  # (tracks, 3)
     last_sample: np.ndarray   # (tracks, 3)
     stats: dict
+    raw_first_sample: Optional[np.ndarray] = None  # before 1/N scaling and direct sound
+    raw_last_sample: Optional[np.ndarray] = None
 
 
 class Tracer:
@@ -214,12 +216,58 @@ class Tracer:
             h.first_sample, h.last_sample = fdev.data_ptr(), ldev.data_ptr()
         else:
             h.first_sample, h.last_sample = first.ctypes.data, last.ctypes.data
+        raw_first = np.zeros((max(tracks, 1), 3), np.int32)
+        raw_last = np.zeros((max(tracks, 1), 3), np.int32)
+        if not h.on_device:
+            h.raw_first_sample, h.raw_last_sample = raw_first.ctypes.data, raw_last.ctypes.data
         st = N.EarRenderStats()
         N.check(N.lib().ear_render(self._h, C.byref(src), recs, len(recorders), C.byref(p),
                                    C.byref(h), C.byref(st)))
         if fdev is not None:
             first, last = fdev.cpu().numpy(), ldev.cpu().numpy()
-        return RenderResult(hist, first[:tracks], last[:tracks], st.as_dict())
+            raw_first = raw_last = None
+        else:
+            raw_first, raw_last = raw_first[:tracks], raw_last[:tracks]
+        return RenderResult(hist, first[:tracks], last[:tracks], st.as_dict(), raw_first, raw_last)
+
+    def set_materials(self, materials: Sequence[Material]) -> None:
+        """Replace the MAT table (same count) without rebuilding the LBVH."""
+        mats = (N.EarMaterial * max(1, len(materials)))()
+        for i, m in enumerate(materials):
+            mats[i] = m.to_c()
+        N.check(N.lib().ear_scene_set_materials(self._h, mats, len(materials)))
+        self.materials = list(materials)
+
+    def render_adjoint(self, source: Source, recorders: Sequence[Recorder], d_hist, *,
+                       first=None, last=None, raw_first=None, raw_last=None, keyframe: int = -1,
+                       **kw):
+        """Gradient of sum(d_hist * h) w.r.t. every material's per-band
+        (absorption, refraction): an array (materials, 3, 2).  ``d_hist`` is a
+        numpy array or CUDA tensor (tracks, 3, num_bins); the bookkeeping of
+        the forward render (RenderResult.first/last/raw_*) is needed unless
+        ``raw=True``."""
+        src, _keep = source.at(keyframe)
+        recs = recorders_at(recorders, keyframe)
+        p = make_params(**kw)
+        on_dev = hasattr(d_hist, "is_cuda") and d_hist.is_cuda
+        if on_dev:
+            d = d_hist.contiguous()
+            ptr = d.data_ptr()
+            if p.stream is None:
+                import torch
+                p.stream = torch.cuda.current_stream(d.device).cuda_stream
+        else:
+            d = np.ascontiguousarray(d_hist, np.float32)
+            ptr = d.ctypes.data
+        grad = np.zeros((len(self.materials), 3, 2), np.float64)
+        keep = [np.ascontiguousarray(x, np.int32) if x is not None else None
+                for x in (raw_first, raw_last, first, last)]
+        ptrs = [k.ctypes.data if k is not None else None for k in keep]
+        st = N.EarRenderStats()
+        N.check(N.lib().ear_render_adjoint(self._h, C.byref(src), recs, len(recorders), C.byref(p),
+                                           ptr, 1 if on_dev else 0, *ptrs, grad.ctypes.data,
+                                           C.byref(st)))
+        return grad, st.as_dict()
 
     def trace_debug(self, source: Source, recorders: Sequence[Recorder], *, band: int,
                     max_record: int, keyframe: int = -1, **kw):

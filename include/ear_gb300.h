@@ -161,6 +161,10 @@ typedef struct ear_histograms {
   int32_t* last_sample;    /* optional, [num_tracks][3] */
   int32_t on_device;       /* data/first/last are device pointers */
   int32_t reserved0;
+  /* optional: the same bookkeeping right after tracing, before the 1/N
+     scaling and the direct sound (what ear_render_adjoint needs) */
+  int32_t* raw_first_sample;
+  int32_t* raw_last_sample;
 } ear_histograms;
 
 /* ---------------------------------------------------------------- errors */
@@ -205,6 +209,36 @@ ear_status ear_trace_debug(ear_scene* scene, const ear_source* source,
                            const ear_render_params* params, int32_t band,
                            int32_t max_record, int32_t* hit_tri,
                            uint8_t* bounce_type, uint32_t* visible);
+
+/* Replaces the MAT table of an existing scene (same count, same order)
+   without touching the geometry or the LBVH -- for optimisation loops over
+   material coefficients.  New: the reference's materials are fixed at parse
+   time (src/Scene.cpp:107-109). */
+ear_status ear_scene_set_materials(ear_scene* scene,
+                                   const ear_material* materials,
+                                   int32_t num_materials);
+
+/* Path-replay adjoint of ear_render.  New: the reference has no
+   derivatives.  With every material parameterised by its per-band
+   absorption a and refraction r (reflection = 1 - a - r), returns
+   grad[material][band][0 = a, 1 = r] = d/d(a, r) of sum(d_hist * h), h being
+   the histograms ear_render produces with the same arguments (same seed,
+   same context: the same paths are re-traced, nothing is stored).  The
+   estimator is exact for the survival product along each path (pathwise)
+   and unbiased for the REFLECT/REFRACT choices (score function); the path
+   cut-off is held fixed.  d_hist: [num_tracks][3][num_bins], host or device
+   (d_hist_on_device).  Unless EAR_FLAG_RAW is set, the finalize scaling is
+   differentiated too, which needs the forward's bookkeeping:
+   raw_first/raw_last (ear_histograms.raw_*) and first/last.  At most 32
+   materials.  grad: host, num_materials * 6 doubles. */
+ear_status ear_render_adjoint(ear_scene* scene, const ear_source* source,
+                              const ear_recorder* recorders,
+                              int32_t num_recorders,
+                              const ear_render_params* params,
+                              const float* d_hist, int32_t d_hist_on_device,
+                              const int32_t* raw_first, const int32_t* raw_last,
+                              const int32_t* first, const int32_t* last,
+                              double* grad, ear_render_stats* stats);
 
 /* ear_render without any allocation.  No counterpart in the reference.
    For callers that must not allocate while rendering: an audio engine that

@@ -40,6 +40,11 @@ def lib():
                                     C.POINTER(N.EarRecorder), C.c_int32,
                                     C.POINTER(N.EarRenderParams), C.c_int32, C.c_int32,
                                     C.POINTER(OracleOutput)]
+        L.oracle_render_adjoint.restype = C.c_int
+        L.oracle_render_adjoint.argtypes = [C.POINTER(N.EarSceneDesc), C.POINTER(N.EarSource),
+                                            C.POINTER(N.EarRecorder), C.c_int32,
+                                            C.POINTER(N.EarRenderParams), C.c_int32, C.c_int32,
+                                            C.c_void_p, C.c_void_p]
         L.oracle_last_error.restype = C.c_char_p
         L.oracle_powf.restype = C.c_float
         L.oracle_powf.argtypes = [C.c_float, C.c_float]
@@ -115,6 +120,27 @@ def render(vertices, material_ids, materials, source, recorders, *, keyframe=-1,
     if dbg is not None:
         out["debug"] = dbg
     return out
+
+
+def adjoint(vertices, material_ids, materials, source, recorders, d_hist, *, keyframe=-1,
+            threads=1, pow_mode=0, **kw):
+    """FP64 path-replay gradient of sum(d_hist * h) with respect to every
+    material's per-band (absorption, refraction), h being ``render``'s
+    finalized histogram with the same arguments: (materials, 3, 2)."""
+    d, keep = scene_desc(vertices, material_ids, materials)
+    src, _k2 = source.at(keyframe)
+    recs = recorders_at(recorders, keyframe)
+    p = make_params(**kw)
+    g = np.ascontiguousarray(d_hist, np.float64)
+    tracks = sum(r.tracks for r in recorders)
+    if g.shape != (tracks, 3, p.num_bins):
+        raise ValueError("d_hist must be (tracks, 3, num_bins)")
+    grad = np.zeros((max(1, len(materials)), 3, 2), np.float64)
+    rc = lib().oracle_render_adjoint(C.byref(d), C.byref(src), recs, len(recorders), C.byref(p),
+                                     int(threads), int(pow_mode), g.ctypes.data, grad.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+    return grad[:len(materials)]
 
 
 def powf(x: float, y: float) -> float:

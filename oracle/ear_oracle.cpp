@@ -209,6 +209,7 @@ struct OMat {
   float p_reflect[3]; // fl2 of Material::Bounce (src/Material.cpp:81)
   bool always_reflect[3];  // src/Material.cpp:79
   float spec[3];
+  float refl[3], refr[3];  // the MAT values (refr = 0 when opaque)
 };
 
 bool derive_material(const ear_material& m, OMat* o) {
@@ -223,6 +224,8 @@ bool derive_material(const ear_material& m, OMat* o) {
     o->always_reflect[i] = ((double)fl < 0.0001 && (double)fr < 0.0001);
     o->p_reflect[i] = fl / (fl + fr);
     o->spec[i] = m.has_specularity ? m.specularity[i] : 0.0f;
+    o->refl[i] = fl;
+    o->refr[i] = fr;
   }
   return true;
 }
@@ -292,12 +295,34 @@ struct OTrack {  // one FloatBuffer (src/Recorder.h:55-92) restricted to a windo
   int64_t last = 0;  // real_length
 };
 
+// Adjoint (path-replay) state.  With absorption a = 1 - refl - refr and
+// refraction r = refr as parameters, a contribution recorded at bounce k
+// carries the survival product of the materials hit (pathwise term) and the
+// probabilities of the REFLECT/REFRACT choices (score term); its gradient
+// in expectation is C * sum_{j<=k} v_j with v_j = grad log(s P(choice)) of
+// the material hit at bounce j.  Summed over contributions this is
+// T * sum_j v_j - sum_j v_j P_j, P_j = sum of contribution gradients before
+// bounce j, T = their total -- accumulated in one forward replay.
+struct Adjoint {
+  const double* g = nullptr;  // dL/d(raw splat sum) [track][band][bin]
+  int nb = 0;
+  int num_mats = 0;
+  std::vector<double> A;      // per ray: sum of v per material, (a, r)
+  double P = 0.0, T = 0.0, G = 0.0;
+  std::vector<double>* grad;  // [material][band][2]
+};
+
 struct Sink {
   int num_bins;
   std::vector<OTrack>* tracks;  // [track][band]
   uint64_t contributions = 0;
+  Adjoint* adj = nullptr;
   // FloatBuffer::operator[] bookkeeping + accumulation (src/Recorder.cpp:52-59)
   inline void sample(int track, int band, int64_t i, float v) {
+    if (adj) {
+      if (i >= 0 && i < num_bins) adj->G += adj->g[((size_t)track * 3 + band) * (size_t)num_bins + i] * (double)v;
+      return;
+    }
     OTrack& tr = (*tracks)[(size_t)track * 3 + band];
     if (i > tr.last) tr.last = i;
     if (i < tr.first) tr.first = i;
@@ -412,6 +437,21 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
   V3 prev_ray_dir = {0.0f, 0.0f, 0.0f};
   V3 o = {0, 0, 0}, d = {0, 0, 0};
   cnt.rays++;
+  Adjoint* adj = sk.adj;
+  if (adj) {
+    std::fill(adj->A.begin(), adj->A.end(), 0.0);
+    adj->P = adj->T = 0.0;
+  }
+  struct Flush {  // at the end of the path: grad += T * A
+    Adjoint* adj;
+    int band;
+    ~Flush() {
+      if (!adj) return;
+      for (int m = 0; m < adj->num_mats; ++m)
+        for (int q = 0; q < 2; ++q)
+          (*adj->grad)[((size_t)m * 3 + band) * 2 + q] += adj->T * adj->A[(size_t)m * 2 + q];
+    }
+  } flush{adj, band};
   for (int k = 0; k <= max_bounces; ++k) {
     V3 n = {0, 0, 0};
     int mat = -1;
@@ -460,6 +500,23 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
       if (!M.always_reflect[band]) {
         const U4 b = rng.block(ray, 0, (uint32_t)k, 0);
         bt = (uniform24(b.v[3]) <= M.p_reflect[band]) ? 0 : 1;
+      }
+      if (adj) {
+        const double fl = M.refl[band], fr = M.refr[band];
+        double va = -1.0 / (double)M.survival[band], vr = 0.0;
+        if (!M.always_reflect[band]) {
+          if (bt == 0) {
+            va += -fr / ((fl + fr) * fl);
+            vr += -1.0 / fl;
+          } else {
+            va += 1.0 / (fl + fr);
+            vr += 1.0 / fr;
+          }
+        }
+        adj->A[(size_t)mat * 2 + 0] += va;
+        adj->A[(size_t)mat * 2 + 1] += vr;
+        (*adj->grad)[((size_t)mat * 3 + band) * 2 + 0] -= va * adj->P;
+        (*adj->grad)[((size_t)mat * 3 + band) * 2 + 1] -= vr * adj->P;
       }
       const float spec = M.spec[band];
       V3 base;
@@ -522,7 +579,12 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
         if (!invalid_float(I)) {
           if (k % 2) I *= -1.0f;
           cnt.contributions++;
+          if (adj) adj->G = 0.0;
           record(sk, rec, band, lsdir, I, (total_path_length + l) / 343.0f, total_path_length + l, pw);
+          if (adj) {
+            adj->P += adj->G;
+            adj->T += adj->G;
+          }
         }
       }
       if (dbg_on && k >= 1 && k <= dbg.max_record) dbg.visible[ray * dbg.max_record + (k - 1)] = vis;
@@ -556,6 +618,12 @@ typedef struct oracle_output {
 
 const char* oracle_last_error(void) { return g_err; }
 
+int ear_num_tracks_oracle(const ear_recorder* r, int32_t n) {
+  int t = 0;
+  for (int i = 0; i < n; ++i) t += r[i].channels == 2 ? 2 : 1;
+  return t;
+}
+
 float oracle_powf(float x, float y) { return portable_powf(x, y); }
 
 void oracle_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
@@ -577,13 +645,19 @@ int oracle_material(const ear_material* m, float* survival, float* p_reflect,
   return 0;
 }
 
+}  // extern "C"
+
+namespace {
+
 // Scene::Render for every band in params->bands_mask (rays of a band are
 // split over num_threads threads in contiguous chunks).  pow_mode 0 =
-// portable_powf, 1 = libm powf.
-int oracle_render(const ear_scene_desc* desc, const ear_source* source,
-                  const ear_recorder* recorders, int32_t num_recorders,
-                  const ear_render_params* params, int32_t num_threads, int32_t pow_mode,
-                  oracle_output* out) {
+// portable_powf, 1 = libm powf.  With adj_g set, the same rays are replayed
+// in adjoint mode instead: nothing is recorded, adj_grad[material][band][2]
+// receives the gradient of sum(adj_g * raw splat sums).
+int render_impl(const ear_scene_desc* desc, const ear_source* source,
+                const ear_recorder* recorders, int32_t num_recorders,
+                const ear_render_params* params, int32_t num_threads, int32_t pow_mode,
+                oracle_output* out, const double* adj_g, double* adj_grad) {
   g_err[0] = 0;
   if (!desc || !source || !params || !out || !out->hist64 || num_recorders < 0 ||
       (num_recorders > 0 && !recorders) || params->num_bins <= 0) {
@@ -677,6 +751,7 @@ int oracle_render(const ear_scene_desc* desc, const ear_source* source,
     const uint64_t N = params->num_rays;
     std::vector<std::vector<OTrack>> priv((size_t)nthreads);
     std::vector<Counters> cnts((size_t)nthreads);
+    std::vector<std::vector<double>> tgrad((size_t)nthreads);
     auto work = [&](int tid) {
       std::vector<OTrack>& pt = priv[(size_t)tid];
       pt.assign(tracks.size(), OTrack());
@@ -687,6 +762,16 @@ int oracle_render(const ear_scene_desc* desc, const ear_source* source,
       Sink sk;
       sk.num_bins = nb;
       sk.tracks = &pt;
+      Adjoint adj;
+      if (adj_g) {
+        adj.g = adj_g;
+        adj.nb = nb;
+        adj.num_mats = (int)sc.mats.size();
+        adj.A.assign(sc.mats.size() * 2, 0.0);
+        adj.grad = &tgrad[(size_t)tid];
+        adj.grad->assign(sc.mats.size() * 3 * 2, 0.0);
+        sk.adj = &adj;
+      }
       const uint64_t lo = N * (uint64_t)tid / (uint64_t)nthreads;
       const uint64_t hi = N * (uint64_t)(tid + 1) / (uint64_t)nthreads;
       for (uint64_t r = lo; r < hi; ++r)
@@ -700,6 +785,9 @@ int oracle_render(const ear_scene_desc* desc, const ear_source* source,
       for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
       for (auto& t : th) t.join();
     }
+    if (adj_g)
+      for (int t = 0; t < nthreads; ++t)
+        for (size_t i = 0; i < tgrad[(size_t)t].size(); ++i) adj_grad[i] += tgrad[(size_t)t][i];
     for (int t = 0; t < nthreads; ++t) {
       for (int tr = 0; tr < num_tracks; ++tr) {
         OTrack& dst = tracks[(size_t)tr * 3 + band];
@@ -773,6 +861,71 @@ int oracle_render(const ear_scene_desc* desc, const ear_source* source,
     out->counters[4] = total.overflows;
   }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_render(const ear_scene_desc* desc, const ear_source* source,
+                  const ear_recorder* recorders, int32_t num_recorders,
+                  const ear_render_params* params, int32_t num_threads, int32_t pow_mode,
+                  oracle_output* out) {
+  return render_impl(desc, source, recorders, num_recorders, params, num_threads, pow_mode, out,
+                     nullptr, nullptr);
+}
+
+// FP64 reference gradient of L = sum(g * h) with respect to each material's
+// per-band absorption and refraction (refl = 1 - absorption - refraction),
+// h being the finalized histogram of oracle_render with the same
+// arguments; grad[material][band][0 = absorption, 1 = refraction].  The
+// finalize steps scale each bin by 1/N when it lies in the pre-direct
+// [first_sample, real_length) and by gain^2 when it lies in the final one
+// (src/Scene.cpp:291,314): the upstream gradient is scaled the same way.
+int oracle_render_adjoint(const ear_scene_desc* desc, const ear_source* source,
+                          const ear_recorder* recorders, int32_t num_recorders,
+                          const ear_render_params* params, int32_t num_threads, int32_t pow_mode,
+                          const double* g, double* grad) {
+  const int nb = params->num_bins;
+  const int tracks = ear_num_tracks_oracle(recorders, num_recorders);
+  const size_t rows = (size_t)tracks * 3;
+  std::vector<double> h64(rows * (size_t)nb), gs(rows * (size_t)nb, 0.0);
+  std::vector<int32_t> f_raw(rows), l_raw(rows), f_fin(rows), l_fin(rows);
+  oracle_output o = {};
+  o.hist64 = h64.data();
+  o.first_sample = f_raw.data();
+  o.last_sample = l_raw.data();
+  ear_render_params raw = *params;
+  raw.flags |= EAR_FLAG_RAW;
+  int rc = render_impl(desc, source, recorders, num_recorders, &raw, num_threads, pow_mode, &o,
+                       nullptr, nullptr);
+  if (rc) return rc;
+  const bool scaled = !(params->flags & EAR_FLAG_RAW);
+  if (scaled) {
+    o.first_sample = f_fin.data();
+    o.last_sample = l_fin.data();
+    rc = render_impl(desc, source, recorders, num_recorders, params, num_threads, pow_mode, &o,
+                     nullptr, nullptr);
+    if (rc) return rc;
+  }
+  const uint64_t N = params->num_rays;
+  const float amount = N <= 16777216ull ? (float)N : 16777216.0f;
+  const double inv = (double)(1.0f / amount);
+  const double gain2 = (double)(source->gain * source->gain);
+  for (size_t r = 0; r < rows; ++r)
+    for (int i = 0; i < nb; ++i) {
+      double sc = 1.0;
+      if (scaled) {
+        if (i >= f_raw[r] && i < l_raw[r]) sc *= inv;
+        if (i >= f_fin[r] && i < l_fin[r]) sc *= gain2;
+      }
+      gs[r * (size_t)nb + i] = g[r * (size_t)nb + i] * sc;
+    }
+  for (int i = 0; i < desc->num_materials * 3 * 2; ++i) grad[i] = 0.0;
+  o = {};
+  o.hist64 = h64.data();
+  return render_impl(desc, source, recorders, num_recorders, params, num_threads, pow_mode, &o,
+                     gs.data(), grad);
 }
 
 // Brute-force query probes (for the traversal parity tests).

@@ -3,12 +3,15 @@ analytic checks and internal consistency.  The reference ships no tests or
 golden vectors for this path, so these are the pins (parity against the
 reference binary itself is unpinned; see oracle/ear_oracle.cpp)."""
 import math
+import os
 
 import numpy as np
 import pytest
 
 import oracle
 from ear_gb300 import Material, Recorder, Source, scenes
+
+THREADS = max(1, min(8, os.cpu_count() or 1))
 
 
 # Philox-4x32-10 known-answer vectors published with Random123 (Salmon et
@@ -180,3 +183,49 @@ def test_sabine_eyring_shoebox():
     assert A == pytest.approx(276.0 * 0.2, rel=1e-4)
     assert sab == pytest.approx(0.1611 * 280 / (276 * 0.2), rel=1e-4)
     assert eyr == pytest.approx(0.1611 * 280 / (-276 * math.log(0.8)), rel=1e-4)
+
+
+def _opaque(a, spec=0.5):
+    return [Material(reflection=tuple((1.0 - a[i]).tolist()), specularity=(spec,) * 3, name=f"m{i}")
+            for i in range(len(a))]
+
+
+def test_oracle_adjoint_pathwise_matches_central_differences():
+    """The FP64 path-replay gradient of sum(g * h) for opaque materials (no
+    parameter-dependent random choice) equals central differences with the
+    same random numbers, after the 1/N and gain^2 finalize scaling."""
+    w, _, _ = scenes.inverse_shoebox()
+    a = np.full((8, 3), 0.2)
+    kw = dict(w.render, num_rays=1500, num_bins=20000)
+    g = np.random.default_rng(3).standard_normal((1, 3, kw["num_bins"]))
+    grad = oracle.adjoint(w.vertices, w.material_ids, _opaque(a), w.source, w.recorders, g,
+                          threads=THREADS, **kw)
+
+    def loss(aa):
+        h = oracle.render(w.vertices, w.material_ids, _opaque(aa), w.source, w.recorders,
+                          threads=THREADS, **kw)["hist64"]
+        return float((h * g).sum())
+
+    for m, b in [(0, 0), (5, 2)]:
+        ap, am = a.copy(), a.copy()
+        ap[m, b] += 1e-3
+        am[m, b] -= 1e-3
+        fd = (loss(ap) - loss(am)) / 2e-3
+        assert grad[m, b, 0] == pytest.approx(fd, rel=1e-3)
+
+
+def test_oracle_adjoint_raw_and_scaled_differ_by_the_finalize_scaling():
+    """With g nonzero only on bins that the direct sound leaves alone, the
+    gradient of the finalized histogram is gain^2 / N times the raw one."""
+    w, _, _ = scenes.inverse_shoebox()
+    mats = [Material(reflection=(0.7, 0.7, 0.7), refraction=(0.1, 0.1, 0.1),
+                     specularity=(0.5,) * 3, name=f"m{i}") for i in range(8)]
+    kw = dict(w.render, num_rays=500, num_bins=20000)
+    g = np.zeros((1, 3, kw["num_bins"]))
+    g[..., 3000:15000] = np.random.default_rng(4).standard_normal((1, 3, 12000))
+    raw = oracle.adjoint(w.vertices, w.material_ids, mats, w.source, w.recorders, g,
+                         threads=THREADS, raw=True, **kw)
+    fin = oracle.adjoint(w.vertices, w.material_ids, mats, w.source, w.recorders, g,
+                         threads=THREADS, **kw)
+    assert np.abs(raw).max() > 0
+    np.testing.assert_allclose(fin, raw / kw["num_rays"], rtol=1e-6, atol=1e-12 * np.abs(raw).max())
