@@ -282,6 +282,96 @@ def adjoint_ratio(device: int, rays: int, steps: int):
             "path": "ear_render (exact) vs ear_render_adjoint (exact, d_hist on device)"}
 
 
+def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_cache=None):
+    """The batched sweep (16 convex rooms of 500..200,000 triangles, 16
+    source / listener pairs each, sources on 24-keyframe paths, 2 s mono
+    histograms, 3 bands) rendered two ways on the same GPU: the plain
+    per-pair loop (one ear_render per pair-frame, histograms to the device)
+    and one autotuned batched launch (ear_batch_run, graph replay).  Point
+    1: every pair-frame at ``rays`` rays per band.  Point 2: one pair-frame
+    per room at ``full_rays`` rays (the configuration's ray count)."""
+    import torch
+
+    from ear_gb300 import Tracer, scenes
+    from ear_gb300.batch import Batch, Job
+
+    rooms, render = scenes.sweep_rooms(keyframes=24)
+    kw = {k: v for k, v in render.items() if k != "num_rays"}
+    dev = torch.device("cuda", device)
+    stream = torch.cuda.current_stream(dev)
+    tracers = [Tracer(r.vertices, r.material_ids, r.materials, device=device) for r in rooms]
+
+    def jobs_for(nrays, kf_list, pairs=None):
+        jobs = []
+        for ri, r in enumerate(rooms):
+            for pi in range(len(r.sources) if pairs is None else pairs):
+                for k in kf_list:
+                    jobs.append(Job(scene=ri, source=r.sources[pi], recorders=[r.listeners[pi]],
+                                    keyframe=k, num_rays=nrays, context=(ri * 16 + pi) * 24 + k))
+        return jobs
+
+    out = torch.zeros((1, 3, render["num_bins"]), dtype=torch.float32, device=dev)
+
+    def plain(jobs):
+        seg = 0
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for j in jobs:
+            r = tracers[j.scene].render(j.source, j.recorders, keyframe=j.keyframe, out=out,
+                                        **dict(kw, num_rays=j.num_rays, context=j.context))
+            seg += int(r.stats["segments"])
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), seg
+
+    def batched(jobs, tune):
+        b = Batch(tracers, jobs, stream=stream.cuda_stream, **kw)
+        t = None
+        if tune:
+            t0 = time.perf_counter()
+            t = b.tune(trial_fraction=0.1, min_trial_rays=128, tune_leaf_size=True,
+                       cache_path=tune_cache)
+            t["tune_s"] = time.perf_counter() - t0
+        b.run()  # capture + first replay
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = b.run()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        cfg = b.config
+        b.close()
+        return ms, int(st["segments"]), cfg, t
+
+    res = {"workload": "sweep: 16 convex rooms (500..200,000 triangles, log-uniform), "
+                       "16 source/listener pairs each, 24-keyframe source paths, 2 s mono, 3 bands",
+           "triangles": [r.num_triangles for r in rooms]}
+    jobs = jobs_for(rays, list(range(keyframes)))
+    bms, bseg, cfg, tune = batched(jobs, True)
+    pms, pseg = plain(jobs)
+    res["all_pair_frames"] = {
+        "pair_frames": len(jobs), "rays_per_pair_frame": rays, "keyframes": keyframes,
+        "plain_ms": pms, "batched_ms": bms, "speedup": pms / bms,
+        "plain_segments_per_s": pseg / (pms / 1000.0), "batched_segments_per_s": bseg / (bms / 1000.0),
+        "segments_equal": pseg == bseg, "schedule": cfg, "tuner": tune}
+    if full_rays:
+        jobs = jobs_for(full_rays, [0], pairs=1)
+        bms, bseg, cfg, _ = batched(jobs, False)
+        pms, pseg = plain(jobs)
+        res["config_rays"] = {
+            "pair_frames": len(jobs), "rays_per_pair_frame": full_rays, "plain_ms": pms,
+            "batched_ms": bms, "speedup": pms / bms,
+            "plain_segments_per_s": pseg / (pms / 1000.0),
+            "batched_segments_per_s": bseg / (bms / 1000.0), "segments_equal": pseg == bseg}
+    for t in tracers:
+        t.close()
+    return res
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -378,6 +468,10 @@ def run_ours(args):
                "path": "ear_scene_create (pinned host) + ear_scene_build_bvh + ear_render "
                        "(histograms to pinned host) + ear_scene_destroy"}
 
+    bat = None
+    if not args.no_batch:
+        bat = batched_sweep(local, args.batch_rays, args.batch_keyframes, args.batch_full_rays)
+
     adj = None
     if not args.no_adjoint:
         adj = adjoint_ratio(local, args.adjoint_rays, max(1, min(args.steps, 5)))
@@ -405,6 +499,7 @@ def run_ours(args):
                          "kernel_ms_per_launch": kern_ms / args.steps},
             "e2e": e2e,
             "adjoint": adj,
+            "batched": bat,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clk,
@@ -429,6 +524,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-rays", type=int, default=2000,
+                    help="rays per band and pair-frame of the batched sweep")
+    ap.add_argument("--batch-keyframes", type=int, default=24)
+    ap.add_argument("--batch-full-rays", type=int, default=1_000_000)
     ap.add_argument("--adjoint-rays", type=int, default=1_000_000)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -43,7 +43,7 @@ class EarSceneDesc(C.Structure):
 
 
 class EarBvhOpts(C.Structure):
-    _fields_ = [("box_pad", C.c_float), ("reserved", C.c_int32 * 7)]
+    _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class EarRecorder(C.Structure):
@@ -79,6 +79,32 @@ class EarHistograms(C.Structure):
                 ("raw_first_sample", C.c_void_p), ("raw_last_sample", C.c_void_p)]
 
 
+class EarBatchJob(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("num_recorders", C.c_int32),
+                ("recorders", C.POINTER(EarRecorder)), ("source", F3), ("gain", C.c_float),
+                ("num_rays", C.c_uint64), ("context", C.c_uint32), ("reserved", C.c_int32)]
+
+
+class EarBatchConfig(C.Structure):
+    _fields_ = [("block", C.c_int32), ("blocks_per_sm", C.c_int32), ("max_leaf_size", C.c_int32),
+                ("no_graph", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+    def as_dict(self):
+        return {"block": self.block, "blocks_per_sm": self.blocks_per_sm,
+                "max_leaf_size": self.max_leaf_size, "no_graph": self.no_graph}
+
+
+class EarTuneOpts(C.Structure):
+    _fields_ = [("trial_fraction", C.c_double), ("min_trial_rays", C.c_uint64),
+                ("tune_leaf_size", C.c_int32), ("repeats", C.c_int32), ("cache_path", C.c_char_p),
+                ("reserved", C.c_int32 * 4)]
+
+
+class EarTuneResult(C.Structure):
+    _fields_ = [("best", EarBatchConfig), ("best_ms", C.c_float), ("default_ms", C.c_float),
+                ("candidates", C.c_int32), ("from_cache", C.c_int32)]
+
+
 # Every exported symbol of include/ear_gb300.h with its ctypes signature.
 SIGNATURES = {
     "ear_last_error": (C.c_char_p, []),
@@ -104,6 +130,20 @@ SIGNATURES = {
     "ear_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder),
                                      C.c_int32, C.POINTER(EarRenderParams), C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.POINTER(EarRenderStats)]),
+    "ear_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(EarBatchJob),
+                                   C.c_int32, C.POINTER(EarRenderParams), C.POINTER(C.c_void_p)]),
+    "ear_batch_set_config": (C.c_int, [C.c_void_p, C.POINTER(EarBatchConfig)]),
+    "ear_batch_get_config": (C.c_int, [C.c_void_p, C.POINTER(EarBatchConfig)]),
+    "ear_batch_set_sources": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ear_batch_run": (C.c_int, [C.c_void_p, C.POINTER(EarRenderStats)]),
+    "ear_batch_histograms": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(EarHistograms)]),
+    "ear_batch_device_view": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int64), C.c_void_p, C.c_int32]),
+    "ear_batch_destroy": (None, [C.c_void_p]),
+    "ear_render_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(EarBatchJob),
+                                   C.c_int32, C.POINTER(EarRenderParams),
+                                   C.POINTER(EarHistograms), C.POINTER(EarRenderStats)]),
+    "ear_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(EarTuneOpts), C.POINTER(EarTuneResult)]),
     "ear_track_power": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),
     "ear_track_maximum": (C.c_float, [C.c_void_p, C.c_int32, C.c_int32]),
     "ear_track_multiply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float]),

@@ -42,6 +42,7 @@ CUDA_UNITS = [
     ("trace_exact.cu", ["--fmad=false"]),
     ("trace_fast.cu", ["--fmad=true"]),
     ("api.cu", ["--fmad=false"]),
+    ("batch.cu", ["--fmad=false"]),
 ]
 CLI_SOURCES = ["cli/ear_cli.cpp", "cli/earfile.cpp"]
 

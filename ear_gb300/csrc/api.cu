@@ -20,21 +20,24 @@
 #include "../../include/ear_gb300.h"
 #include "ear_internal.h"
 #include "ear_record.cuh"
+#include "host_internal.h"
 
 namespace ear {
-size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block) {
-  size_t b = sizeof(DevMaterial) * (size_t)num_mats + sizeof(int) * 6 * (size_t)num_tracks;
+
+// Layout of the trace kernel's dynamic shared memory: the material table
+// (16-byte aligned), then per (track, band) first/last bookkeeping for a
+// single render or the scene table for a batch, then the adjoint's
+// accumulators.
+size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block, int num_scenes) {
+  size_t b = (sizeof(DevMaterial) * (size_t)num_mats + 15) & ~(size_t)15;
+  if (mode == kModeBatch) return b + sizeof(SceneRef) * (size_t)num_scenes;
+  b += sizeof(int) * 6 * (size_t)num_tracks;
   if (mode == kModeAdjoint) {
     b = (b + 7) & ~(size_t)7;
     b += sizeof(double) * 6 * (size_t)num_mats + sizeof(float) * 2 * (size_t)num_mats * (size_t)block;
   }
   return b;
 }
-}  // namespace ear
-
-using namespace ear;
-
-namespace {
 
 thread_local char g_err[512] = "";
 
@@ -45,14 +48,6 @@ ear_status fail(ear_status st, const char* fmt, ...) {
   va_end(ap);
   return st;
 }
-
-#define CU(x)                                                                             \
-  do {                                                                                    \
-    cudaError_t e_ = (x);                                                                 \
-    if (e_ != cudaSuccess)                                                                \
-      return fail(e_ == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,  \
-                  "%s: %s", #x, cudaGetErrorString(e_));                                  \
-  } while (0)
 
 // Material::Material (src/Material.cpp:26-72) and Material::Bounce
 // (src/Material.cpp:76-83), per band.
@@ -75,16 +70,48 @@ bool derive_material(const ear_material& m, DevMaterial* o) {
   return true;
 }
 
-template <typename T>
-cudaError_t grow(T** p, size_t* cap, size_t n) {
-  if (n <= *cap && *p) return cudaSuccess;
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-  *cap = 0;
-  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) *cap = n;
-  return e;
+int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job,
+                     std::vector<DevRecorder>* out) {
+  int tracks = 0;
+  for (int i = 0; i < nrec; ++i) {
+    const ear_recorder& r = recs[i];
+    if (r.channels != 1 && r.channels != 2) {
+      fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
+      return -1;
+    }
+    DevRecorder d;
+    for (int k = 0; k < 3; ++k) {
+      d.loc[k] = r.location[k];
+      d.right[k] = r.right_ear[k];
+      // std::max(0.0f, powf(1.0f - h, 4)) (src/StereoRecorder.cpp:56)
+      const float h = powf_portable(1.0f - r.head_absorption[k], 4.0f);
+      d.habs[k] = (0.0f < h) ? h : 0.0f;
+    }
+    d.head_size = r.head_size;
+    d.channels = r.channels;
+    d.track0 = track_base + tracks;
+    d.job = job;
+    tracks += r.channels;
+    out->push_back(d);
+  }
+  return tracks;
 }
+
+void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel_ms,
+                ear_render_stats* stats) {
+  if (!stats) return;
+  stats->rays = std::min<unsigned long long>(cnt[kWork], num_items);
+  stats->segments = cnt[kSegments];
+  stats->shadow_queries = cnt[kShadow];
+  stats->contributions = cnt[kContrib];
+  stats->sampler_overflows = cnt[kOverflow];
+  stats->node_visits = cnt[kNodeVisits];
+  stats->triangle_tests = cnt[kTriTests];
+  stats->splat_bins = cnt[kSplatBins];
+  stats->kernel_ms = kernel_ms;
+}
+
+namespace fin {
 
 __global__ void k_init_first_last(int2* fl, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -98,20 +125,6 @@ __global__ void k_init_first_last(int2* fl, int n) {
 // trace kernel found the listener-source segment unblocked, then
 // Multiply(gain^2).  The block owns its rows, so the lobe is added with
 // plain stores by one thread, in the reference's order.
-struct FinalizeArgs {
-  float* hist;
-  int stride;
-  int num_bins;
-  int2* first_last;
-  const DevRecorder* recs;
-  const int* direct_vis;  // null: no direct sound
-  float src[3];
-  float air[3];
-  float dry;
-  float inv_amount;
-  float gain2;
-  uint32_t bands;
-};
 
 __device__ void scale_rows(const FinalizeArgs& f, const DevRecorder& R, int band, float x) {
   for (int k = 0; k < R.channels; ++k) {
@@ -127,11 +140,19 @@ __global__ void k_finalize(const FinalizeArgs f) {
   const int ri = blockIdx.x / 3, band = blockIdx.x % 3;
   if (!((f.bands >> band) & 1u)) return;
   const DevRecorder R = f.recs[ri];
-  scale_rows(f, R, band, f.inv_amount);
+  const float* sp = f.src;
+  float inv_amount = f.inv_amount, gain2 = f.gain2;
+  if (f.jobs) {
+    const BatchJob& J = f.jobs[R.job];
+    sp = J.src;
+    inv_amount = J.inv_amount;
+    gain2 = J.gain2;
+  }
+  scale_rows(f, R, band, inv_amount);
   __syncthreads();
   if (threadIdx.x == 0 && f.direct_vis && f.direct_vis[ri]) {
     const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
-    const V3 src = mk(f.src[0], f.src[1], f.src[2]);
+    const V3 src = mk(sp[0], sp[1], sp[2]);
     const V3 dist = sub(loc, src);
     const float len = length(dist);
     const V3 dir = normalized(dist);
@@ -156,35 +177,28 @@ __global__ void k_finalize(const FinalizeArgs f) {
     }
   }
   __syncthreads();
-  scale_rows(f, R, band, f.gain2);
+  scale_rows(f, R, band, gain2);
 }
 
-}  // namespace
+}  // namespace fin
 
-struct ear_scene {
-  int device = 0;
-  DeviceScene ds;
-  int num_mats = 0;
-  DevMaterial* mats = nullptr;
-  bool bvh = false;
-  int sm_count = 0;
-  // render scratch, grown on demand and reused
-  float* hist = nullptr;
-  size_t hist_cap = 0;
-  int2* fl = nullptr;
-  size_t fl_cap = 0;
-  unsigned long long* counters = nullptr;
-  size_t counters_cap = 0;
-  int* err = nullptr;
-  size_t err_cap = 0;
-  int* dvis = nullptr;
-  size_t dvis_cap = 0;
-  DevRecorder* recs = nullptr;
-  size_t recs_cap = 0;
-  float4* emitter = nullptr;
-  size_t emitter_cap = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-};
+using namespace fin;
+
+cudaError_t launch_init_first_last(int2* fl, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_init_first_last<<<(n + 127) / 128, 128, 0, st>>>(fl, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FinalizeArgs& f, int num_recorders, cudaStream_t st) {
+  if (num_recorders <= 0) return cudaSuccess;
+  k_finalize<<<num_recorders * 3, 256, 0, st>>>(f);
+  return cudaGetLastError();
+}
+
+}  // namespace ear
+
+using namespace ear;
 
 extern "C" {
 
@@ -259,7 +273,9 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   CU(cudaSetDevice(s->device));
   char msg[256] = "";
   const float pad = opts ? opts->box_pad : -1.0f;
-  cudaError_t e = build_lbvh(s->ds, pad, 0, msg, sizeof msg);
+  const int max_leaf = opts && opts->max_leaf_size > 0 ? opts->max_leaf_size : 1;
+  if (max_leaf > 16) return fail(EAR_ERR_INVALID_ARG, "max_leaf_size above 16");
+  cudaError_t e = build_lbvh(s->ds, pad, max_leaf, 0, msg, sizeof msg);
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
@@ -311,6 +327,7 @@ struct Prepared {
   int num_tracks;
   size_t smem;
   int grid;
+  int block;
   const TraceOps* ops;
 };
 
@@ -327,25 +344,9 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   if (p->num_rays > (1ull << 47)) return fail(EAR_ERR_INVALID_ARG, "num_rays above 2^47");
   if (src->num_emitter_triangles < 0 || (src->num_emitter_triangles > 0 && !src->emitter_vertices))
     return fail(EAR_ERR_INVALID_ARG, "bad emitter triangles");
-  std::vector<DevRecorder> dr((size_t)nrec);
-  int tracks = 0;
-  for (int i = 0; i < nrec; ++i) {
-    const ear_recorder& r = recs[i];
-    if (r.channels != 1 && r.channels != 2)
-      return fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
-    DevRecorder& d = dr[(size_t)i];
-    for (int k = 0; k < 3; ++k) {
-      d.loc[k] = r.location[k];
-      d.right[k] = r.right_ear[k];
-      // std::max(0.0f, powf(1.0f - h, 4)) (src/StereoRecorder.cpp:56)
-      const float h = powf_portable(1.0f - r.head_absorption[k], 4.0f);
-      d.habs[k] = (0.0f < h) ? h : 0.0f;
-    }
-    d.head_size = r.head_size;
-    d.channels = r.channels;
-    d.track0 = tracks;
-    tracks += r.channels;
-  }
+  std::vector<DevRecorder> dr;
+  const int tracks = derive_recorders(recs, nrec, 0, 0, &dr);
+  if (tracks < 0) return EAR_ERR_INVALID_ARG;
   TraceArgs& a = out->a;
   std::memset(&a, 0, sizeof a);
   const bool exact = (p->flags & EAR_FLAG_EXACT) != 0;
@@ -376,7 +377,7 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   a.num_bins = p->num_bins;
   a.stride = (p->num_bins + 3) & ~3;
   a.num_tracks = tracks;
-  a.traverse_budget = (int)std::min<int64_t>(4 * s->ds.num_nodes + 64, (int64_t)1 << 30);
+  a.traverse_budget = traverse_budget(s->ds.num_nodes);
   a.dbg_band = -1;
   out->num_tracks = tracks;
 
@@ -428,10 +429,11 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
     k_init_first_last<<<(tracks * 3 + 127) / 128, 128, 0, st>>>(s->fl, tracks * 3);
     CU(cudaGetLastError());
   }
-  out->smem = trace_smem_bytes(s->num_mats, tracks, mode, out->ops->block);
+  out->block = out->ops->block;
+  out->smem = trace_smem_bytes(s->num_mats, tracks, mode, out->block);
   if (out->smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
   int per_sm = 0;
-  CU(out->ops->occupancy(mode, out->smem, &per_sm));
+  CU(out->ops->occupancy(mode, out->block, out->smem, &per_sm));
   if (per_sm < 1) per_sm = 1;
   out->grid = s->sm_count * per_sm;
   return EAR_OK;
@@ -469,7 +471,7 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
   cudaStream_t st = (cudaStream_t)p->stream;
   CU(cudaEventRecord(s->ev0, st));
   // with no rays the launch still computes the direct-sound visibility
-  CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.smem, kModeForward, st));
+  CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.block, pr.smem, kModeForward, st));
   CU(cudaEventRecord(s->ev1, st));
   const int rows = pr.num_tracks * 3;
   std::vector<int2> fl_raw((size_t)std::max(rows, 1));
@@ -480,7 +482,7 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
     // amount is a float incremented once per ray (src/Scene.cpp:122,127):
     // exact to 2^24 rays, then stuck at 2^24.
     const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
-    FinalizeArgs f;
+    FinalizeArgs f = {};
     f.hist = a.hist;
     f.stride = a.stride;
     f.num_bins = a.num_bins;
@@ -570,7 +572,7 @@ extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
     a.dbg_bt = db;
     a.dbg_vis = dv;
     e = cudaEventRecord(s->ev0, st);
-    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, kModeDebug, st);
+    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.block, pr.smem, kModeDebug, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(hit_tri, dh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(bounce_type, db, n, cudaMemcpyDeviceToHost, st);
@@ -681,7 +683,7 @@ extern "C" ear_status ear_render_adjoint(ear_scene* s, const ear_source* src,
     a.adj_g = a.hist;
     a.adj_grad = dgrad;
     e = cudaEventRecord(s->ev0, st);
-    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.smem, kModeAdjoint, st);
+    if (e == cudaSuccess && a.num_items > 0) e = pr.ops->trace(a, pr.grid, pr.block, pr.smem, kModeAdjoint, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
   }
   unsigned long long cnt[kNumCounters] = {0};
@@ -897,6 +899,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     d.head_size = r.head_size;
     d.channels = r.channels;
     d.track0 = tracks;
+    d.job = 0;
     tracks += r.channels;
   }
   CU(cudaSetDevice(s->device));
@@ -941,7 +944,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.direct_vis = direct ? reinterpret_cast<int*>(scratch + kNaVis) : nullptr;
   a.counters = reinterpret_cast<unsigned long long*>(scratch + kNaCounters);
   a.error_flag = reinterpret_cast<int*>(scratch + kNaError);
-  a.traverse_budget = (int)std::min<int64_t>(4 * s->ds.num_nodes + 64, (int64_t)1 << 30);
+  a.traverse_budget = traverse_budget(s->ds.num_nodes);
   a.dbg_band = -1;
 
   cudaStream_t st = (cudaStream_t)p->stream;
@@ -957,14 +960,14 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   const size_t smem = trace_smem_bytes(s->num_mats, tracks, kModeForward, ops->block);
   if (smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
   int per_sm = 0;
-  CU(ops->occupancy(kModeForward, smem, &per_sm));
+  CU(ops->occupancy(kModeForward, ops->block, smem, &per_sm));
   if (per_sm < 1) per_sm = 1;
   CU(cudaEventRecord(s->ev0, st));
-  CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, smem, kModeForward, st));
+  CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, ops->block, smem, kModeForward, st));
   CU(cudaEventRecord(s->ev1, st));
   if (!(p->flags & EAR_FLAG_RAW) && nrec > 0) {
     const float amount = p->num_rays <= 16777216ull ? (float)p->num_rays : 16777216.0f;
-    FinalizeArgs f;
+    FinalizeArgs f = {};
     f.hist = hist;
     f.stride = p->num_bins;
     f.num_bins = p->num_bins;

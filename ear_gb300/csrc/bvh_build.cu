@@ -100,7 +100,7 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, int n, 
 
 // One thread per internal node (Karras 2012, Fig. 4).
 __global__ void k_karras(const uint32_t* __restrict__ codes, int n, Node* __restrict__ nodes,
-                         int32_t* __restrict__ leaf_parent) {
+                         int32_t* __restrict__ leaf_parent, int2* __restrict__ range) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const int d = (delta(codes, n, i, i + 1) - delta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -119,6 +119,7 @@ __global__ void k_karras(const uint32_t* __restrict__ codes, int n, Node* __rest
   } while (t > 1);
   const int gamma = i + s * d + (d < 0 ? d : 0);
   const int first = i < j ? i : j, last = i < j ? j : i;
+  range[i] = make_int2(first, last);
   int c0, c1;
   if (first == gamma) {
     c0 = ~gamma;
@@ -177,6 +178,26 @@ __global__ void k_refit(const float4* __restrict__ lo, const float4* __restrict_
   }
 }
 
+// Leaf collapse: an internal child whose subtree spans at most max_leaf
+// triangles (a contiguous range of the sorted order) becomes one leaf over
+// that range.  Its box in the parent is already the union of the subtree.
+// The nodes below it stay in memory but are no longer reachable.
+__global__ void k_collapse(const int2* __restrict__ range, int n, int max_leaf, Node* nodes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int4 d = nodes[i].d;
+  int c[2] = {d.x, d.y};
+  for (int k = 0; k < 2; ++k) {
+    if (c[k] < 0) continue;
+    const int2 r = range[c[k]];
+    const int cnt = r.y - r.x + 1;
+    if (cnt <= max_leaf) c[k] = ~(r.x | ((cnt - 1) << kLeafCountShift));
+  }
+  d.x = c[0];
+  d.y = c[1];
+  nodes[i].d = d;
+}
+
 // Depth of every leaf (internal nodes on its root path + 1).
 __global__ void k_depth(const int32_t* __restrict__ leaf_parent, int n, const Node* __restrict__ nodes,
                         int* max_depth) {
@@ -228,8 +249,8 @@ __global__ void k_single(const float4* __restrict__ lo, const float4* __restrict
 
 }  // namespace
 
-cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char* err,
-                       size_t errlen) {
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t stream,
+                       char* err, size_t errlen) {
   const int64_t n64 = s.num_tris;
   cudaError_t rc = cudaSuccess;
   err[0] = 0;
@@ -241,6 +262,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char*
   float4 *lo = nullptr, *hi = nullptr, *node_lo = nullptr, *node_hi = nullptr;
   uint32_t *bounds = nullptr, *codes = nullptr, *codes2 = nullptr, *visits = nullptr;
   int32_t *idx = nullptr, *idx2 = nullptr, *leaf_parent = nullptr;
+  int2* range = nullptr;
   int* dmax = nullptr;
   void* tmp = nullptr;
   size_t tmp_bytes = 0;
@@ -273,6 +295,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char*
   CK(cudaMalloc(&node_lo, sizeof(float4) * nn));
   CK(cudaMalloc(&node_hi, sizeof(float4) * nn));
   CK(cudaMalloc(&visits, sizeof(uint32_t) * nn));
+  CK(cudaMalloc(&range, sizeof(int2) * nn));
   CK(cudaMalloc(&dmax, sizeof(int)));
   CK(cudaMalloc(&s.nodes, sizeof(Node) * nn));
   CK(cudaMalloc(&s.tris, sizeof(float4) * 3 * (size_t)n));
@@ -308,13 +331,17 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char*
     CK(cudaMalloc(&tmp, tmp_bytes));
     CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, codes, codes2, idx, idx2, n, 0, 30,
                                        stream));
-    k_karras<<<(nn + B - 1) / B, B, 0, stream>>>(codes2, n, s.nodes, leaf_parent);
+    k_karras<<<(nn + B - 1) / B, B, 0, stream>>>(codes2, n, s.nodes, leaf_parent, range);
     CK(cudaGetLastError());
     k_refit<<<G, B, 0, stream>>>(lo, hi, idx2, leaf_parent, n, s.box_pad, s.nodes, node_lo,
                                  node_hi, visits);
     CK(cudaGetLastError());
     k_depth<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, dmax);
     CK(cudaGetLastError());
+    if (max_leaf > 1) {
+      k_collapse<<<(nn + B - 1) / B, B, 0, stream>>>(range, n, max_leaf, s.nodes);
+      CK(cudaGetLastError());
+    }
     CK(cudaMemcpyAsync(&depth, dmax, sizeof(int), cudaMemcpyDeviceToHost, stream));
   }
   k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris, s.nrm);
@@ -322,6 +349,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char*
   CK(cudaStreamSynchronize(stream));
   s.num_nodes = nn;
   s.max_depth = depth;
+  s.max_leaf = max_leaf;
   if (depth > 62) {
     snprintf(err, errlen, "LBVH depth %d exceeds the 62 levels of the traversal trail", depth);
     rc = cudaErrorInvalidValue;
@@ -338,6 +366,7 @@ done:
   cudaFree(node_lo);
   cudaFree(node_hi);
   cudaFree(visits);
+  cudaFree(range);
   cudaFree(dmax);
   cudaFree(tmp);
   return rc;

@@ -32,6 +32,7 @@ struct DeviceScene {
   int64_t num_nodes = 0;
   int max_depth = 0;
   float box_pad = 0.0f;
+  int max_leaf = 1;
   Node* nodes = nullptr;
   float4* tris = nullptr;
   float4* nrm = nullptr;
@@ -58,7 +59,36 @@ struct DevRecorder {
   float head_size;
   float habs[3];
   int channels;
-  int track0;
+  int track0;  // first histogram track (global over a batch)
+  int job;     // batch job the recorder belongs to (0 outside batches)
+};
+
+// One scene as the trace kernel addresses it.  A batch keeps a table of
+// these in shared memory; a single render builds one from its TraceArgs.
+struct __align__(16) SceneRef {
+  const Node* nodes;
+  const float4* tris;
+  const float4* nrm;
+  int num_tris;
+  int num_nodes;
+  float box_pad;
+  int mat_base;  // first material of the scene in the launch's table
+  int num_mats;
+  int traverse_budget;
+};
+
+// One (scene, source position, recorder set) of a batch.  Its work items
+// are bands x num_rays, numbered from item_end of the previous job.
+struct BatchJob {
+  uint64_t num_rays;
+  float src[3];
+  uint32_t context;
+  int scene;
+  int rec_base;  // first recorder in the launch's recorder table
+  int num_recs;
+  float inv_amount;  // 1 / (float ray count), for the finalize step
+  float gain2;
+  int pad[3];
 };
 
 // Everything one trace launch needs, passed by value (param space).
@@ -98,6 +128,12 @@ struct TraceArgs {
   // and the gradient accumulators [material][band][2 = absorption, refraction]
   const float* adj_g;
   double* adj_grad;
+  // batch mode: scene and job tables, cumulative item ends per job
+  const SceneRef* scenes;
+  int num_scenes;
+  const BatchJob* jobs;
+  const uint64_t* job_end;
+  int num_jobs;
   unsigned long long* counters;  // [0] work, [1] segments, [2] shadow, [3] contrib, [4] overflow
   int* error_flag;
   int traverse_budget;
@@ -125,17 +161,23 @@ enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 
 // LBVH build (bvh_build.cu).  Returns a cudaError_t; `err` receives a
 // message on failure.
-cudaError_t build_lbvh(DeviceScene& s, float box_pad, cudaStream_t stream, char* err, size_t errlen);
+// Subtrees of at most max_leaf (1..16) triangles become one leaf.
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t stream, char* err,
+                       size_t errlen);
 
 // Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
-enum TraceMode { kModeForward = 0, kModeDebug = 1, kModeAdjoint = 2 };
+// kModeBatch traces many jobs (scene, source, recorders) from one work
+// counter; the others trace one.
+enum TraceMode { kModeForward = 0, kModeDebug = 1, kModeAdjoint = 2, kModeBatch = 3 };
+constexpr int kTraceMaxBlock = 256;
 struct TraceOps {
-  cudaError_t (*trace)(const TraceArgs& a, int grid, size_t smem, int mode, cudaStream_t s);
-  cudaError_t (*occupancy)(int mode, size_t smem, int* blocks_per_sm);
-  int block;
+  cudaError_t (*trace)(const TraceArgs& a, int grid, int block, size_t smem, int mode,
+                       cudaStream_t s);
+  cudaError_t (*occupancy)(int mode, int block, size_t smem, int* blocks_per_sm);
+  int block;  // default block size
 };
 // Dynamic shared memory of a trace launch.
-size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block);
+size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block, int num_scenes = 0);
 extern const TraceOps kTraceExact;
 extern const TraceOps kTraceFast;
 

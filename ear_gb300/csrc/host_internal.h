@@ -1,0 +1,111 @@
+// host_internal.h -- host-side pieces shared by the C-ABI translation units
+// (api.cu: scenes and single renders; batch.cu: batched renders and the
+// autotuner): error reporting, the derived per-material / per-recorder
+// constants, the scene object and the end-of-render kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/ear_gb300.h"
+#include "ear_internal.h"
+
+namespace ear {
+
+// Thread-local message returned by ear_last_error.
+extern thread_local char g_err[512];
+ear_status fail(ear_status st, const char* fmt, ...);
+
+#define CU(x)                                                                             \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess)                                                                \
+      return ::ear::fail(e_ == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY          \
+                                                         : EAR_ERR_CUDA,                  \
+                         "%s: %s", #x, cudaGetErrorString(e_));                           \
+  } while (0)
+
+// Material::Material (src/Material.cpp:26-72), per band.
+bool derive_material(const ear_material& m, DevMaterial* o);
+
+// MonoRecorder / StereoRecorder constructors (src/StereoRecorder.cpp:53-57):
+// appends one DevRecorder per recorder with tracks numbered from
+// track_base; `job` is stored in each.  Returns the number of tracks, or
+// -1 (with the error set) for an invalid recorder.
+int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job,
+                     std::vector<DevRecorder>* out);
+
+template <typename T>
+cudaError_t grow(T** p, size_t* cap, size_t n) {
+  if (n <= *cap && *p) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+// End of Scene::Render for every (recorder, band): 1/amount scaling, the
+// direct sound, gain^2.  With `jobs` set, the source, 1/amount and gain^2
+// of each recorder's batch job replace the single-render values.
+struct FinalizeArgs {
+  float* hist;
+  int stride;
+  int num_bins;
+  int2* first_last;
+  const DevRecorder* recs;
+  const int* direct_vis;  // null: no direct sound
+  const BatchJob* jobs;   // null: single render
+  float src[3];
+  float air[3];
+  float dry;
+  float inv_amount;
+  float gain2;
+  uint32_t bands;
+};
+
+cudaError_t launch_init_first_last(int2* fl, int n, cudaStream_t st);
+cudaError_t launch_finalize(const FinalizeArgs& f, int num_recorders, cudaStream_t st);
+
+// float ray count of Scene::Render (src/Scene.cpp:122,127): exact to 2^24
+// rays, then stuck at 2^24.
+inline float ray_amount(uint64_t num_rays) {
+  return num_rays <= 16777216ull ? (float)num_rays : 16777216.0f;
+}
+
+inline int traverse_budget(int64_t num_nodes) {
+  return (int)std::min<int64_t>(4 * num_nodes + 64, (int64_t)1 << 30);
+}
+
+void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel_ms,
+                ear_render_stats* stats);
+
+}  // namespace ear
+
+struct ear_scene {
+  int device = 0;
+  ear::DeviceScene ds;
+  int num_mats = 0;
+  ear::DevMaterial* mats = nullptr;
+  bool bvh = false;
+  int sm_count = 0;
+  // render scratch, grown on demand and reused
+  float* hist = nullptr;
+  size_t hist_cap = 0;
+  int2* fl = nullptr;
+  size_t fl_cap = 0;
+  unsigned long long* counters = nullptr;
+  size_t counters_cap = 0;
+  int* err = nullptr;
+  size_t err_cap = 0;
+  int* dvis = nullptr;
+  size_t dvis_cap = 0;
+  ear::DevRecorder* recs = nullptr;
+  size_t recs_cap = 0;
+  float4* emitter = nullptr;
+  size_t emitter_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};

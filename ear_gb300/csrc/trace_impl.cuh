@@ -14,6 +14,13 @@
 // (__syncwarp) after every data-dependent loop.  BVH traversal is
 // stackless: a 64-bit trail records, per level of the current root path,
 // whether the far child is still pending; backtracking climbs parent links.
+//
+// Batch mode (kModeBatch) runs the same loop over many jobs -- (scene,
+// source position, recorders) triples of a sweep over rooms, source /
+// listener pairs and keyframes -- from one work counter: a refilled lane
+// finds its job by binary search over the jobs' cumulative item ends and
+// keeps the job's scene, RNG context and recorder range in registers; the
+// scenes' node / triangle pointers come from a table in shared memory.
 #pragma once
 
 #ifndef EAR_NS
@@ -29,7 +36,6 @@ namespace ear {
 namespace EAR_NS {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kTraceBlock = 256;
 
 struct Ray {
   float ox, oy, oz;
@@ -107,11 +113,11 @@ __device__ __forceinline__ int clamp_index(int idx, int n, int& err) {
 
 // Returns true (ANY) when the segment is blocked.
 template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3 d, Hit& h,
+__device__ __forceinline__ bool leaf_test(const SceneRef& S, int code, V3 o, V3 d, Hit& h,
                                           LaneCounters& c, int& err) {
   int start = (~code) & kLeafStartMask;
   int cnt = ((~code) >> kLeafCountShift) + 1;
-  if ((unsigned)(start + cnt - 1) >= (unsigned)a.num_tris) {
+  if ((unsigned)(start + cnt - 1) >= (unsigned)S.num_tris) {
     err |= kErrIndex;
     start = 0;
     cnt = 1;
@@ -119,7 +125,7 @@ __device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3
   c.tris += (uint32_t)cnt;
   bool blocked = false;
   for (int k = 0; k < cnt; ++k) {
-    const float4* T = a.tris + 3 * (start + k);
+    const float4* T = S.tris + 3 * (start + k);
     const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
     float t;
     if (mt_intersect(A, B, C, o, d, t)) {
@@ -145,25 +151,25 @@ __device__ __forceinline__ bool leaf_test(const TraceArgs& a, int code, V3 o, V3
 // Any hit (ANY = true): returns true when blocked.  `slack` widens the
 // t-range culling so rounding in the slab test never removes a candidate.
 template <bool ANY>
-__device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float slack, Hit& h,
+__device__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slack, Hit& h,
                          LaneCounters& c, int& err) {
   h.t = tlimit;
   h.pos = -1;
   h.orig = INT_MAX;
-  if (a.num_tris == 0) return false;
+  if (S.num_tris == 0) return false;
   const Ray r = make_ray(o, d);
   int cur = 0;
   unsigned long long trail = 1ull;
   int iters = 0;
-  const Node* __restrict__ nodes = a.nodes;
+  const Node* __restrict__ nodes = S.nodes;
   bool blocked = false;
   const int err0 = err;
   for (;;) {
-    if (++iters > a.traverse_budget) {
+    if (++iters > S.traverse_budget) {
       err |= kErrBudget;
       break;
     }
-    cur = clamp_index(cur, a.num_nodes, err);
+    cur = clamp_index(cur, S.num_nodes, err);
     const Node* nd = nodes + cur;
     c.nodes++;
     const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
@@ -173,11 +179,11 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
     if (h0 && ch.x < 0) {
-      blocked |= leaf_test<ANY>(a, ch.x, o, d, h, c, err);
+      blocked |= leaf_test<ANY>(S, ch.x, o, d, h, c, err);
       h0 = false;
     }
     if (h1 && ch.y < 0) {
-      blocked |= leaf_test<ANY>(a, ch.y, o, d, h, c, err);
+      blocked |= leaf_test<ANY>(S, ch.y, o, d, h, c, err);
       h1 = false;
     }
     if (ANY && blocked) break;
@@ -200,14 +206,14 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
       }
       if (trail & 1ull) {
         trail ^= 1ull;
-        const int par = clamp_index(__ldg(&nodes[cur].d.z), a.num_nodes, err);
+        const int par = clamp_index(__ldg(&nodes[cur].d.z), S.num_nodes, err);
         const int4 pc = __ldg(&nodes[par].d);
         cur = (pc.x == cur) ? pc.y : pc.x;
         break;
       }
       trail >>= 1;
-      cur = clamp_index(__ldg(&nodes[cur].d.z), a.num_nodes, err);
-      if (++iters > a.traverse_budget) {
+      cur = clamp_index(__ldg(&nodes[cur].d.z), S.num_nodes, err);
+      if (++iters > S.traverse_budget) {
         err |= kErrBudget;
         done = true;
         break;
@@ -226,12 +232,13 @@ __device__ bool traverse(const TraceArgs& a, V3 o, V3 d, float tlimit, float sla
 // Sample_Sphere / Sample_Hemi (src/Distributions.h:48-67): one Philox
 // block per try; try 0's block is passed in (its 4th word also drives the
 // material choice).
-__device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t band, uint64_t ray,
-                                           uint32_t bounce, bool hemi, V3 n, U4 b, V3& out) {
+__device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t ctx, uint32_t band,
+                                           uint64_t ray, uint32_t bounce, bool hemi, V3 n, U4 b,
+                                           V3& out) {
   bool ok = false;
   out = mk(0.0f, 0.0f, 1.0f);
   for (int tr = 0; tr < kMaxTries; ++tr) {
-    if (tr) b = rng_block(a.k0, a.k1, a.context, band, ray, 0, bounce, (uint32_t)tr);
+    if (tr) b = rng_block(a.k0, a.k1, ctx, band, ray, 0, bounce, (uint32_t)tr);
     const float f1 = uniform24(b.x) * 2.0f - 1.0f;
     const float f2 = uniform24(b.y) * 2.0f - 1.0f;
     const float f3 = uniform24(b.z) * 2.0f - 1.0f;
@@ -260,8 +267,12 @@ __device__ __forceinline__ void splat(float* row, int* first, int* last, int nb,
   const long long lastpos = s + w - 1;
   if (lastpos < 0) return;
   const long long firstpos = s < 0 ? 0 : s;
-  atomicMin(first, (int)(firstpos < nb ? firstpos : nb));
-  atomicMax(last, (int)(lastpos < nb ? lastpos : nb));
+  // first only decreases and last only increases, so a stale read can only
+  // cause a redundant atomic, never a missed one
+  const int fp = (int)(firstpos < nb ? firstpos : nb);
+  const int lp = (int)(lastpos < nb ? lastpos : nb);
+  if (fp < *(volatile int*)first) atomicMin(first, fp);
+  if (lp > *(volatile int*)last) atomicMax(last, lp);
   if (firstpos >= nb) return;
   float v = ampl;
   float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -315,8 +326,12 @@ __device__ __forceinline__ float record(const TraceArgs& a, const DevRecorder& R
       G += gather(a.adj_g + (size_t)tb * (size_t)a.stride, a.num_bins, p.s[k], p.w, p.ampl[k],
                   p.step[k]);
     } else {
-      splat(a.hist + (size_t)tb * (size_t)a.stride, s_first + tb, s_last + tb, a.num_bins, p.s[k],
-            p.w, p.ampl[k], p.step[k], bins);
+      // single render: bookkeeping privatised in shared memory, merged once
+      // per block; batch: straight to the global rows
+      int* fp = MODE == kModeBatch ? reinterpret_cast<int*>(a.first_last + tb) : s_first + tb;
+      int* lp = MODE == kModeBatch ? fp + 1 : s_last + tb;
+      splat(a.hist + (size_t)tb * (size_t)a.stride, fp, lp, a.num_bins, p.s[k], p.w, p.ampl[k],
+            p.step[k], bins);
     }
   }
   return G;
@@ -330,7 +345,32 @@ struct PathState {
   int band;
   uint64_t ray;
   float P, T;  // adjoint: gradient weights of the contributions so far / in total
+  // batch mode: the lane's job
+  int job, scene, rec_base, num_recs;
+  uint32_t ctx;
 };
+
+template <int MODE>
+__device__ __forceinline__ uint32_t ctx_of(const TraceArgs& a, const PathState& st) {
+  return MODE == kModeBatch ? st.ctx : a.context;
+}
+
+template <int MODE>
+__device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef* s_scenes,
+                                             const PathState& st) {
+  if (MODE == kModeBatch) return s_scenes[st.scene];
+  SceneRef S;
+  S.nodes = a.nodes;
+  S.tris = a.tris;
+  S.nrm = a.nrm;
+  S.num_tris = a.num_tris;
+  S.num_nodes = a.num_nodes;
+  S.box_pad = a.box_pad;
+  S.mat_base = 0;
+  S.num_mats = a.num_mats;
+  S.traverse_budget = a.traverse_budget;
+  return S;
+}
 
 // Adjoint bookkeeping in shared memory: per thread, the per-material sums
 // A[m] of v_j = grad log(weight of the choice at bounce j) -- the weight of
@@ -353,16 +393,18 @@ struct Vertex {
 // Visibility + contribution of recorder `ri` at the current vertex
 // (src/Scene.cpp:188-268).  Returns whether the recorder is visible.
 template <int MODE>
-__device__ __forceinline__ bool connect_one(const TraceArgs& a, PathState& st, const Vertex& vx,
-                                            int ri, LaneCounters& c, int& err, int* s_first,
+__device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* s_scenes,
+                                            PathState& st, const Vertex& vx, int ri,
+                                            LaneCounters& c, int& err, int* s_first,
                                             int* s_last) {
-  const DevRecorder& R = a.recs[ri];
+  const DevRecorder& R = a.recs[(MODE == kModeBatch ? st.rec_base : 0) + ri];
   const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
   c.shadow++;
   const float len = length(sdir);
   Hit hh;
-  const float slack = 2.44140625e-4f + a.box_pad / len;
-  if (traverse<true>(a, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
+  const SceneRef S = scene_of<MODE>(a, s_scenes, st);
+  const float slack = 2.44140625e-4f + S.box_pad / len;
+  if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
   const int k = st.k;
   const V3 lsdir = normalized(sdir);
   const float dt = k ? dot(lsdir, vx.n) : 1.0f;
@@ -429,10 +471,11 @@ __device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, 
     for (int m = 0; m < 2 * a.num_mats; ++m) adj.A[m] = 0.0f;
   }
   const uint32_t band = (uint32_t)st.band;
-  const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, 0, 0);
-  if (a.num_emitter > 0) {
+  const uint32_t ctx = ctx_of<MODE>(a, st);
+  const U4 b0 = rng_block(a.k0, a.k1, ctx, band, st.ray, 0, 0, 0);
+  if (MODE != kModeBatch && a.num_emitter > 0) {
     // Mesh::SamplePoint (src/Mesh.cpp:143-154): linear walk of the area CDF
-    const U4 e = rng_block(a.k0, a.k1, a.context, band, st.ray, 1, 0, 0);
+    const U4 e = rng_block(a.k0, a.k1, ctx, band, st.ray, 1, 0, 0);
     float x = uniform24(e.x) * a.emitter_total_area;
     V3 p = mk(0, 0, 0), en = mk(0, 0, 0);
     for (int i = 0; i < a.num_emitter; ++i) {
@@ -451,16 +494,21 @@ __device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, 
       }
     }
     st.o = p;
-    if (!sample_dir(a, band, st.ray, 0, true, en, b0, st.d)) c.overflow++;
+    if (!sample_dir(a, ctx, band, st.ray, 0, true, en, b0, st.d)) c.overflow++;
   } else {
-    st.o = mk(a.src[0], a.src[1], a.src[2]);
-    if (!sample_dir(a, band, st.ray, 0, false, mk(0, 0, 0), b0, st.d)) c.overflow++;
+    if (MODE == kModeBatch) {
+      const float* js = a.jobs[st.job].src;
+      st.o = mk(js[0], js[1], js[2]);
+    } else {
+      st.o = mk(a.src[0], a.src[1], a.src[2]);
+    }
+    if (!sample_dir(a, ctx, band, st.ray, 0, false, mk(0, 0, 0), b0, st.d)) c.overflow++;
   }
   vx.n = mk(0, 0, 0);
   vx.bt = 0;
   vx.spec = 0.0f;
   vx.before = st.I;
-  vx.conn = a.num_emitter > 0;
+  vx.conn = MODE != kModeBatch && a.num_emitter > 0;
 }
 
 // Reflection k = st.k + 1 up to the recorder connections
@@ -468,24 +516,26 @@ __device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, 
 // air and surface losses.  Returns whether the path continues.
 template <int MODE>
 __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict__ mats,
-                              PathState& st, LaneCounters& c, int& err, Vertex& vx,
-                              const AdjShared& adj) {
+                              const SceneRef* s_scenes, PathState& st, LaneCounters& c, int& err,
+                              Vertex& vx, const AdjShared& adj) {
   const int k = st.k + 1;
   const uint32_t band = (uint32_t)st.band;
   c.segments++;
   Hit h;
-  traverse<false>(a, st.o, st.d, 1000000.0f, a.box_pad, h, c, err);
+  const SceneRef S = scene_of<MODE>(a, s_scenes, st);
+  traverse<false>(S, st.o, st.d, 1000000.0f, S.box_pad, h, c, err);
   debug_put<MODE>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
-  const float4 nm = __ldg(a.nrm + h.pos);
+  const float4 nm = __ldg(S.nrm + h.pos);
   const float t = h.t;
   const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
   const V3 N = mk(nm.x, nm.y, nm.z);
   V3 n = (dot(N, st.d) > 0.0f) ? neg(N) : N;
-  const int mid = clamp_index(__float_as_int(nm.w), a.num_mats, err);
+  const int mid = clamp_index(__float_as_int(nm.w), S.num_mats, err) + S.mat_base;
   const DevMaterial& M = mats[mid];
   // Material::Bounce (src/Material.cpp:76-83)
-  const U4 b0 = rng_block(a.k0, a.k1, a.context, band, st.ray, 0, (uint32_t)k, 0);
+  const uint32_t ctx = ctx_of<MODE>(a, st);
+  const U4 b0 = rng_block(a.k0, a.k1, ctx, band, st.ray, 0, (uint32_t)k, 0);
   int bt = 0;
   if (!((M.always_reflect >> band) & 1u)) bt = (uniform24(b0.w) <= M.p_reflect[band]) ? 0 : 1;
   debug_put<MODE>(a, st, k, 0, bt, 0, 1);
@@ -522,7 +572,7 @@ __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict_
     base = reflect(st.d, n);
   }
   V3 v;
-  if (!sample_dir(a, band, st.ray, (uint32_t)k, true, n, b0, v)) c.overflow++;
+  if (!sample_dir(a, ctx, band, st.ray, (uint32_t)k, true, n, b0, v)) c.overflow++;
   const float om = 1.0f - spec;
   v = normalized(mk(v.x * om + base.x * spec, v.y * om + base.y * spec, v.z * om + base.z * spec));
   const float l = length(sub(p, st.o));
@@ -557,29 +607,53 @@ __device__ __forceinline__ void adjoint_flush(const TraceArgs& a, const PathStat
 // source) for every recorder, computed by the first threads of block 0
 // with the same any-hit traversal as the path connections.  The lobe
 // itself is added by the finalize kernel between the two scaling passes.
-__device__ void direct_visibility(const TraceArgs& a, int& err) {
-  const int r = (int)threadIdx.x;
-  if (blockIdx.x != 0 || r >= a.num_recs || a.direct_vis == nullptr) return;
-  const DevRecorder& R = a.recs[r];
-  const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
-  const V3 seg = sub(mk(a.src[0], a.src[1], a.src[2]), loc);
-  const float seglen = length(seg);
-  const float slack = 2.44140625e-4f + (seglen > 0.0f ? a.box_pad / seglen : 0.0f);
-  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
-  Hit hh;
-  const bool blocked = traverse<true>(a, loc, seg, 1.0f, slack, hh, c, err);
-  a.direct_vis[r] = blocked ? 0 : 1;
+// A batch spreads its (job, recorder) pairs over every thread of the grid.
+template <int MODE>
+__device__ void direct_visibility(const TraceArgs& a, const SceneRef* s_scenes, int& err) {
+  if (a.direct_vis == nullptr) return;
+  int r = (int)threadIdx.x;
+  int step = a.num_recs;
+  if (MODE == kModeBatch) {
+    r += (int)(blockIdx.x * blockDim.x);
+    step = (int)(gridDim.x * blockDim.x);
+  } else if (blockIdx.x != 0) {
+    return;
+  }
+  for (; r < a.num_recs; r += step) {
+    const DevRecorder& R = a.recs[r];
+    const float* src = a.src;
+    PathState st;
+    st.scene = 0;
+    if (MODE == kModeBatch) {
+      const BatchJob& J = a.jobs[R.job];
+      src = J.src;
+      st.scene = J.scene;
+    }
+    const SceneRef S = scene_of<MODE>(a, s_scenes, st);
+    const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
+    const V3 seg = sub(mk(src[0], src[1], src[2]), loc);
+    const float seglen = length(seg);
+    const float slack = 2.44140625e-4f + (seglen > 0.0f ? S.box_pad / seglen : 0.0f);
+    LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
+    Hit hh;
+    const bool blocked = traverse<true>(S, loc, seg, 1.0f, slack, hh, c, err);
+    a.direct_vis[r] = blocked ? 0 : 1;
+  }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
+__global__ void __launch_bounds__(kTraceMaxBlock) trace_kernel(const TraceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevMaterial* s_mats = reinterpret_cast<DevMaterial*>(smem_raw);
-  int* s_first = reinterpret_cast<int*>(smem_raw + sizeof(DevMaterial) * a.num_mats);
+  const size_t mat_bytes = (sizeof(DevMaterial) * (size_t)a.num_mats + 15) & ~(size_t)15;
+  // single render: first/last bookkeeping per (track, band); batch: the
+  // scene table
+  int* s_first = reinterpret_cast<int*>(smem_raw + mat_bytes);
   int* s_last = s_first + a.num_tracks * 3;
+  SceneRef* s_scenes = reinterpret_cast<SceneRef*>(smem_raw + mat_bytes);
   AdjShared adj = {nullptr, nullptr};
   if (MODE == kModeAdjoint) {
-    size_t off = sizeof(DevMaterial) * a.num_mats + sizeof(int) * 6 * a.num_tracks;
+    size_t off = mat_bytes + sizeof(int) * 6 * a.num_tracks;
     off = (off + 7) & ~(size_t)7;
     adj.grad = reinterpret_cast<double*>(smem_raw + off);
     float* all_A = reinterpret_cast<float*>(adj.grad + 6 * a.num_mats);
@@ -591,14 +665,22 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
     uint32_t* dst = reinterpret_cast<uint32_t*>(s_mats);
     const int words = (int)(sizeof(DevMaterial) / 4) * a.num_mats;
     for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
-    for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
-      s_first[i] = kInitialFirstSample;
-      s_last[i] = 0;
+    if (MODE == kModeBatch) {
+      const uint32_t* ssrc = reinterpret_cast<const uint32_t*>(a.scenes);
+      uint32_t* sdst = reinterpret_cast<uint32_t*>(s_scenes);
+      const int swords = (int)(sizeof(SceneRef) / 4) * a.num_scenes;
+      for (int i = threadIdx.x; i < swords; i += blockDim.x) sdst[i] = __ldg(ssrc + i);
+    } else {
+      for (int i = threadIdx.x; i < a.num_tracks * 3; i += blockDim.x) {
+        s_first[i] = kInitialFirstSample;
+        s_last[i] = 0;
+      }
     }
   }
   int err = 0;
-  direct_visibility(a, err);
+  if (MODE != kModeBatch) direct_visibility<MODE>(a, s_scenes, err);
   __syncthreads();
+  if (MODE == kModeBatch) direct_visibility<MODE>(a, s_scenes, err);
   const int lane = threadIdx.x & 31;
   LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
   bool alive = false, exhausted = false;
@@ -608,6 +690,11 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
   st.ray = 0;
   st.P = 0.0f;
   st.T = 0.0f;
+  st.job = 0;
+  st.scene = 0;
+  st.rec_base = 0;
+  st.num_recs = 0;
+  st.ctx = 0;
   // Every lane, live or not, passes the same __syncwarp() points below;
   // per-lane work between them is predicated, so divergent loops
   // (traversal, rejection sampling) reconverge at each phase boundary.
@@ -623,9 +710,34 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
       if (!alive && !exhausted) {
         const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
         if (w < a.num_items) {
-          const uint64_t bi = w / a.num_rays;
-          st.band = a.bands[bi < 3 ? bi : 0];
-          st.ray = w - bi * a.num_rays;
+          if (MODE == kModeBatch) {
+            // the job whose item range holds w: first job with w < end
+            int lo = 0, hi = a.num_jobs - 1;
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (w < __ldg(a.job_end + mid)) {
+                hi = mid;
+              } else {
+                lo = mid + 1;
+              }
+            }
+            const uint64_t begin = lo ? __ldg(a.job_end + lo - 1) : 0ull;
+            const BatchJob& J = a.jobs[lo];
+            const uint64_t nr = J.num_rays;
+            const uint64_t local = w - begin;
+            const uint64_t bi = local / nr;
+            st.band = a.bands[bi < 3 ? bi : 0];
+            st.ray = local - bi * nr;
+            st.job = lo;
+            st.scene = J.scene;
+            st.rec_base = J.rec_base;
+            st.num_recs = J.num_recs;
+            st.ctx = J.context;
+          } else {
+            const uint64_t bi = w / a.num_rays;
+            st.band = a.bands[bi < 3 ? bi : 0];
+            st.ray = w - bi * a.num_rays;
+          }
           fresh = true;
         } else {
           exhausted = true;
@@ -641,15 +753,19 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
       emit_vertex<MODE>(a, st, c, vx, adj);
       alive = true;
     } else if (alive) {
-      alive = bounce_vertex<MODE>(a, s_mats, st, c, err, vx, adj);
+      alive = bounce_vertex<MODE>(a, s_mats, s_scenes, st, c, err, vx, adj);
       vx.conn = alive;
       if (MODE == kModeAdjoint && !alive) adjoint_flush(a, st, adj);
     }
     __syncwarp();
     // phase 3: recorder connections (src/Scene.cpp:185-270)
     uint32_t vis = 0;
-    for (int ri = 0; ri < a.num_recs; ++ri) {
-      if (vx.conn && connect_one<MODE>(a, st, vx, ri, c, err, s_first, s_last))
+    const int nrec = MODE == kModeBatch
+                         ? (int)__reduce_max_sync(kFull, vx.conn ? (unsigned)st.num_recs : 0u)
+                         : a.num_recs;
+    for (int ri = 0; ri < nrec; ++ri) {
+      if (vx.conn && (MODE != kModeBatch || ri < st.num_recs) &&
+          connect_one<MODE>(a, s_scenes, st, vx, ri, c, err, s_first, s_last))
         vis |= 1u << (ri & 31);
       __syncwarp();
     }
@@ -686,6 +802,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs a) {
       if (werr) atomicOr(a.error_flag, werr);
     }
   }
+  if (MODE == kModeBatch) return;
   __syncthreads();
   if (MODE == kModeAdjoint) {
     for (int i = threadIdx.x; i < 6 * a.num_mats; i += blockDim.x)

@@ -356,3 +356,118 @@ def small_test_room(seed: int = 3, n_side: int = 4) -> Workload:
         recorders=recs,
         render=dict(num_rays=2000, max_bounces=60, num_bins=SR, cutoff=1e-6,
                     air_absorption=(0.01, 0.02, 0.05), dry=1.0, seed=seed))
+
+
+# ------------------------------------------------------------------ sweep
+@dataclass
+class SweepRoom:
+    """One room of the batched sweep: a convex polyhedron with subdivided
+    faces, its materials, and source / listener pairs (the source animated
+    over keyframes)."""
+    name: str
+    vertices: np.ndarray          # (n, 9) float32, outward normals
+    material_ids: np.ndarray      # (n,) int32
+    materials: List[Material]
+    sources: List[Source]         # per pair, location (keyframes, 3)
+    listeners: List[Recorder]     # per pair, mono
+    halfspaces: np.ndarray        # (faces, 4): n.x + d <= 0 inside
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.vertices.shape[0])
+
+
+def _subdivide(tris: np.ndarray, levels: int) -> np.ndarray:
+    """Midpoint 4-split of every triangle, `levels` times (stays planar,
+    keeps the winding)."""
+    t = tris.reshape(-1, 3, 3)
+    for _ in range(levels):
+        a, b, c = t[:, 0], t[:, 1], t[:, 2]
+        ab, bc, ca = (a + b) * 0.5, (b + c) * 0.5, (c + a) * 0.5
+        t = np.stack([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1),
+                      np.stack([ca, bc, c], 1), np.stack([ab, bc, ca], 1)], 1).reshape(-1, 3, 3)
+    return t.reshape(-1, 9)
+
+
+def _inside(h: np.ndarray, p: np.ndarray, margin: float) -> bool:
+    return bool(np.all(h[:, :3] @ p + h[:, 3] <= -margin))
+
+
+def convex_room(rng, target_tris: int, n_mats: int, name: str = "room") -> SweepRoom:
+    """Random convex polyhedron: the hull of points on a random ellipsoid
+    (half-axes 4..15 m), faces 4-split until the triangle count is near
+    ``target_tris``; one random material per hull face."""
+    from scipy.spatial import ConvexHull
+
+    levels = 0
+    while target_tris / (4 ** levels) > 2000:
+        levels += 1
+    faces = max(8, int(round(target_tris / (4 ** levels))))
+    npts = faces // 2 + 2
+    radii = rng.uniform(4.0, 15.0, 3)
+    d = rng.standard_normal((npts, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pts = d * radii + radii  # corner of the bounding box at the origin
+    hull = ConvexHull(pts)
+    centre = pts.mean(0)
+    simp = hull.simplices.copy()
+    P = pts[simp]  # (F, 3, 3)
+    n = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0])
+    flip = np.einsum("ij,ij->i", n, P.mean(1) - centre) < 0
+    simp[flip] = simp[flip][:, [0, 2, 1]]
+    tris = pts[simp].reshape(-1, 9)
+    face_mat = rng.integers(0, n_mats, len(simp))
+    v = _subdivide(tris, levels).astype(np.float32)
+    ids = np.repeat(face_mat, 4 ** levels).astype(np.int32)
+    absorb = rng.uniform(0.02, 0.6, size=(n_mats, 3))
+    refr = rng.uniform(0.0, 0.1, size=(n_mats, 3))
+    spec = rng.uniform(0.1, 0.9, size=(n_mats, 3))
+    mats = [Material(reflection=tuple((1.0 - absorb[i] - refr[i]).tolist()),
+                     refraction=tuple(refr[i].tolist()), specularity=tuple(spec[i].tolist()),
+                     name=f"{name}-m{i}") for i in range(n_mats)]
+    return SweepRoom(name=name, vertices=v, material_ids=ids, materials=mats, sources=[],
+                     listeners=[], halfspaces=hull.equations.astype(np.float64))
+
+
+def _point_inside(rng, room: SweepRoom, margin: float) -> np.ndarray:
+    lo = room.vertices.reshape(-1, 3).min(0)
+    hi = room.vertices.reshape(-1, 3).max(0)
+    for _ in range(100000):
+        p = rng.uniform(lo, hi)
+        if _inside(room.halfspaces, p, margin):
+            return p
+    raise RuntimeError("no interior point found")
+
+
+def sweep_rooms(num_rooms: int = 16, pairs_per_room: int = 16, keyframes: int = 24,
+                path_length: float = 5.0, min_tris: int = 500, max_tris: int = 200_000,
+                seed: int = 3):
+    """The batched sweep: ``num_rooms`` convex rooms whose triangle counts
+    are log-uniform in [min_tris, max_tris], 4-8 materials each, and
+    ``pairs_per_room`` source / listener pairs placed uniformly inside
+    (0.5 m from the walls); each source moves along a random straight
+    ``path_length`` m path sampled at ``keyframes`` keyframes.  Render
+    settings: 2 s mono histograms, 3 bands, 200 reflections, cut-off 1e-8,
+    1e6 rays per pair-frame.  Returns (rooms, render settings)."""
+    rng = np.random.default_rng(seed)
+    rooms = []
+    for r in range(num_rooms):
+        target = int(round(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris)))))
+        room = convex_room(rng, target, int(rng.integers(4, 9)), name=f"sweep{r}")
+        for _ in range(pairs_per_room):
+            for _try in range(1000):
+                a = _point_inside(rng, room, 0.5)
+                u = rng.standard_normal(3)
+                u /= np.linalg.norm(u)
+                b = a + path_length * u
+                if _inside(room.halfspaces, b, 0.5):
+                    break
+            else:
+                raise RuntimeError("no source path fits inside the room")
+            t = np.linspace(0.0, 1.0, keyframes)[:, None]
+            room.sources.append(Source(location=((1 - t) * a + t * b).astype(np.float32)))
+            room.listeners.append(Recorder(location=_point_inside(rng, room, 0.5).astype(np.float32)))
+        rooms.append(room)
+    render = dict(num_rays=1_000_000, max_bounces=200, num_bins=2 * SR, cutoff=1e-8,
+                  air_absorption=(0.01, 0.02, 0.05), dry=1.0, seed=seed)
+    return rooms, render

@@ -98,7 +98,11 @@ typedef struct ear_bvh_opts {
      1e-5).  Padding only makes the culling conservative; it never changes
      which triangle is reported. */
   float box_pad;
-  int32_t reserved[7];
+  /* Subtrees of at most this many triangles (1..16; 0 = 1) become one leaf:
+     fewer node visits, more triangle tests per visit.  Never changes which
+     triangle is reported. */
+  int32_t max_leaf_size;
+  int32_t reserved[6];
 } ear_bvh_opts;
 
 /* OUT1 (mono, src/MonoRecorder.cpp:38-59) or OUT2 (stereo,
@@ -239,6 +243,98 @@ ear_status ear_render_adjoint(ear_scene* scene, const ear_source* source,
                               const int32_t* raw_first, const int32_t* raw_last,
                               const int32_t* first, const int32_t* last,
                               double* grad, ear_render_stats* stats);
+
+/* ---------------------------------------------------------- batches
+ * Many renders -- rooms (scenes) x source/listener pairs x keyframes x
+ * bands -- traced by ONE persistent launch that pulls (job, band, ray) work
+ * items from a device counter, replayed as a captured CUDA graph.  No
+ * counterpart in the reference, which renders one (source, keyframe, band)
+ * per Scene::Render call (src/EAR.cpp:225-243); every job of a batch gives
+ * the same rays as ear_render with the batch's seed and the job's context,
+ * scene, source and recorders. */
+typedef struct ear_batch ear_batch;
+
+typedef struct ear_batch_job {
+  int32_t scene;                 /* index into the scenes of ear_batch_create */
+  int32_t num_recorders;         /* 1..32 */
+  const ear_recorder* recorders; /* host; evaluated at this job's keyframe */
+  float source[3];               /* point source position at the keyframe */
+  float gain;                    /* SSRC gain, squared into the response */
+  uint64_t num_rays;             /* rays per band (> 0) */
+  uint32_t context;              /* RNG context, as ear_render_params.context */
+  int32_t reserved;
+} ear_batch_job;
+
+/* Launch schedule of a batch; every field 0 selects the default. */
+typedef struct ear_batch_config {
+  int32_t block;          /* threads per block: 32..256, multiple of 32 (256) */
+  int32_t blocks_per_sm;  /* resident blocks per SM, i.e. rays in flight per
+                             SM; capped at the occupancy limit (limit) */
+  int32_t max_leaf_size;  /* BVH leaf size the batch's scenes are built with;
+                             set by ear_batch_tune (read-only otherwise) */
+  int32_t no_graph;       /* 1: launch directly instead of replaying the
+                             captured CUDA graph */
+  int32_t reserved[4];
+} ear_batch_config;
+
+/* Plans a batch: validates the jobs, derives the recorder constants,
+   allocates the device job tables and one histogram row per (job, track,
+   band).  The scenes (with their LBVH built, all on one device) must
+   outlive the batch.  From `params`: seed, bands_mask, max_bounces,
+   num_bins, cutoff, air_absorption, dry_level, flags (EXACT, RAW,
+   NO_DIRECT) and stream; num_rays and context come from each job. */
+ear_status ear_batch_create(ear_scene* const* scenes, int32_t num_scenes,
+                            const ear_batch_job* jobs, int32_t num_jobs,
+                            const ear_render_params* params, ear_batch** out);
+ear_status ear_batch_set_config(ear_batch* batch, const ear_batch_config* config);
+ear_status ear_batch_get_config(const ear_batch* batch, ear_batch_config* config);
+/* Moves every job's point source ([num_jobs][3], host) without re-planning;
+   the next run replays the same graph. */
+ear_status ear_batch_set_sources(ear_batch* batch, const float* positions);
+/* Renders every job (histograms stay on the device) and waits for it.
+   stats (optional) sums the batch; kernel_ms is the device time of the
+   whole launch sequence. */
+ear_status ear_batch_run(ear_batch* batch, ear_render_stats* stats);
+/* Job `job`'s finalized tracks after ear_batch_run, as ear_render returns
+   them (raw_first_sample / raw_last_sample are not reported). */
+ear_status ear_batch_histograms(const ear_batch* batch, int32_t job, ear_histograms* out);
+/* Device view of all rows: data[row * stride + bin], rows = 3 * tracks of
+   the batch; job `job`'s rows start at 3 * first_track[job]. */
+ear_status ear_batch_device_view(const ear_batch* batch, const float** data, int32_t* stride,
+                                 int64_t* rows, int32_t* first_track, int32_t max_jobs);
+void ear_batch_destroy(ear_batch* batch);
+
+/* One-shot: ear_batch_create + ear_batch_run + ear_batch_histograms for
+   every job (outs[num_jobs]) + ear_batch_destroy. */
+ear_status ear_render_batch(ear_scene* const* scenes, int32_t num_scenes,
+                            const ear_batch_job* jobs, int32_t num_jobs,
+                            const ear_render_params* params, ear_histograms* outs,
+                            ear_render_stats* stats);
+
+/* Autotuner.  Times trial launches of the batch -- every job with a
+   fraction of its rays -- over the schedule space (block size x blocks per
+   SM, and with tune_leaf_size the BVH leaf size, which rebuilds the
+   batch's scenes) and applies the fastest.  With cache_path, results are
+   kept in that text file under a key of the device and the batch's shape
+   and are reused without timing. */
+typedef struct ear_tune_opts {
+  double trial_fraction;   /* of each job's rays per trial (0 = 0.02) */
+  uint64_t min_trial_rays; /* per job and trial (0 = 256) */
+  int32_t tune_leaf_size;  /* 1: also try leaf sizes 1, 2, 4, 8 */
+  int32_t repeats;         /* timed runs per candidate, best kept (0 = 2) */
+  const char* cache_path;  /* NULL: no persistent cache */
+  int32_t reserved[4];
+} ear_tune_opts;
+
+typedef struct ear_tune_result {
+  ear_batch_config best;
+  float best_ms;      /* trial time of the chosen schedule */
+  float default_ms;   /* trial time of the default schedule */
+  int32_t candidates; /* schedules timed */
+  int32_t from_cache; /* 1: taken from cache_path without timing */
+} ear_tune_result;
+
+ear_status ear_batch_tune(ear_batch* batch, const ear_tune_opts* opts, ear_tune_result* result);
 
 /* ear_render without any allocation.  No counterpart in the reference.
    For callers that must not allocate while rendering: an audio engine that

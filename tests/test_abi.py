@@ -42,7 +42,9 @@ def test_ctypes_layout_matches_c():
         "ear_material": N.EarMaterial, "ear_scene_desc": N.EarSceneDesc,
         "ear_bvh_opts": N.EarBvhOpts, "ear_recorder": N.EarRecorder, "ear_source": N.EarSource,
         "ear_render_params": N.EarRenderParams, "ear_render_stats": N.EarRenderStats,
-        "ear_histograms": N.EarHistograms,
+        "ear_histograms": N.EarHistograms, "ear_batch_job": N.EarBatchJob,
+        "ear_batch_config": N.EarBatchConfig, "ear_tune_opts": N.EarTuneOpts,
+        "ear_tune_result": N.EarTuneResult,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ear_gb300.h"', "int main(){"]
     for cname, py in structs.items():
@@ -103,3 +105,11 @@ def test_track_functions_match_oracle():
             oracle.lib().oracle_track_length(b.ctypes.data, len(b), first, last, tr)
     assert N.lib().ear_track_t60(a.ctypes.data, first, last) == \
         oracle.lib().oracle_track_t60(b.ctypes.data, first, last)
+
+
+def test_batch_arguments_are_checked_before_device_work():
+    h = C.c_void_p()
+    p = N.EarRenderParams()
+    assert N.lib().ear_batch_create(None, 0, None, 0, C.byref(p), C.byref(h)) == N.EAR_ERR_INVALID_ARG
+    assert N.lib().ear_batch_run(None, None) == N.EAR_ERR_INVALID_ARG
+    assert N.lib().ear_batch_tune(None, None, None) == N.EAR_ERR_INVALID_ARG
