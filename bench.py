@@ -331,7 +331,7 @@ def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_c
         t = None
         if tune:
             t0 = time.perf_counter()
-            t = b.tune(trial_fraction=0.1, min_trial_rays=128, tune_leaf_size=True,
+            t = b.tune(trial_fraction=0.05, min_trial_rays=64, tune_leaf_size=True, repeats=1,
                        cache_path=tune_cache)
             t["tune_s"] = time.perf_counter() - t0
         b.run()  # capture + first replay

@@ -628,8 +628,8 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
   CU(cudaMemcpy(b->d_trial_end, tend.data(), sizeof(uint64_t) * tend.size(), cudaMemcpyHostToDevice));
 
   std::vector<int> leaves = {b->cfg.max_leaf_size > 0 ? b->cfg.max_leaf_size : 1};
-  if (o.tune_leaf_size) leaves = {1, 2, 4, 8};
-  const int blocks[] = {64, 128, 256};
+  if (o.tune_leaf_size) leaves = {1, 2, 4};
+  const int blocks[] = {128, 256};
   ear_batch_config best{};
   float best_ms = 0.0f;
   bool have = false;
@@ -645,9 +645,11 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
       Schedule sc;
       ear_status rc = schedule(b, probe, &sc);
       if (rc != EAR_OK) return rc;
+      // resident blocks per SM: the occupancy limit, one less, and half
       const int max_per_sm = sc.grid / b->sm_count;
       std::vector<int> per = {max_per_sm};
-      for (int q = 1; q < max_per_sm; q *= 2) per.push_back(q);
+      if (max_per_sm > 1) per.push_back(max_per_sm - 1);
+      if (max_per_sm > 3) per.push_back(max_per_sm / 2);
       for (int q : per) {
         ear_batch_config c{};
         c.block = block;

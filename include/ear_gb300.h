@@ -320,7 +320,7 @@ ear_status ear_render_batch(ear_scene* const* scenes, int32_t num_scenes,
 typedef struct ear_tune_opts {
   double trial_fraction;   /* of each job's rays per trial (0 = 0.02) */
   uint64_t min_trial_rays; /* per job and trial (0 = 256) */
-  int32_t tune_leaf_size;  /* 1: also try leaf sizes 1, 2, 4, 8 */
+  int32_t tune_leaf_size;  /* 1: also try leaf sizes 1, 2, 4 */
   int32_t repeats;         /* timed runs per candidate, best kept (0 = 2) */
   const char* cache_path;  /* NULL: no persistent cache */
   int32_t reserved[4];

@@ -99,7 +99,7 @@ def test_autotuner_applies_a_schedule_and_changes_no_result(sweep, tmp_path):
         assert res["candidates"] >= 4 and not res["from_cache"]
         assert res["best_ms"] > 0 and res["default_ms"] > 0
         cfg = b.config
-        assert cfg["max_leaf_size"] in (1, 2, 4, 8) and cfg["block"] in (64, 128, 256)
+        assert cfg["max_leaf_size"] in (1, 2, 4) and cfg["block"] in (128, 256)
         _check(b, plain, b.run())
     # a second batch of the same shape takes the cached schedule
     with Batch(tracers, jobs, exact=True, **kw) as b:
