@@ -387,7 +387,8 @@ def run_ours(args):
     kw = dict(w.render)
     kw["seed"] = int(kw.get("seed", 0)) + rank
     exact = args.exact
-    tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad)
+    tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad,
+                    builder=args.builder)
     tracks = w.num_tracks
     out = torch.zeros((tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -453,7 +454,8 @@ def run_ours(args):
         e_seg = 0
         e0.record(stream)
         for _ in range(e_steps):
-            t2 = Tracer(vp, mp, w.materials, device=local, box_pad=args.box_pad)
+            t2 = Tracer(vp, mp, w.materials, device=local, box_pad=args.box_pad,
+                        builder=args.builder)
             r2 = t2.render(w.source, w.recorders, out=host_out, exact=exact, **kw)
             t2.close()
             e_seg += int(r2.stats["segments"])
@@ -485,6 +487,7 @@ def run_ours(args):
     if rank == 0:
         cfg = _config(w, args, flush="flushed before every step (512 MB write)")
         cfg["mode"] = "exact (--fmad=false)" if exact else "fast"
+        cfg["bvh"] = tracer.info()
         cfg["rays_per_s"] = agg["rays"] / (total_ms / 1000.0) * world
         line = {
             "metric": "ray-bounce segments/s", "value": value, "unit": "segments/s",
@@ -521,6 +524,7 @@ def main():
     ap.add_argument("--cpu-rays", type=int, default=None)
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--box-pad", type=float, default=-1.0)
+    ap.add_argument("--builder", default="default", choices=["default", "lbvh", "ploc"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

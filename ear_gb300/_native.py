@@ -24,6 +24,10 @@ EAR_FLAG_EXACT = 0x1
 EAR_FLAG_RAW = 0x2
 EAR_FLAG_NO_DIRECT = 0x4
 
+EAR_BVH_DEFAULT = 0
+EAR_BVH_LBVH = 1
+EAR_BVH_PLOC = 2
+
 EAR_REFERENCE_MAX_BOUNCES = 999
 EAR_REFERENCE_CUTOFF = 1e-8
 SAMPLE_RATE = 44100
@@ -43,7 +47,8 @@ class EarSceneDesc(C.Structure):
 
 
 class EarBvhOpts(C.Structure):
-    _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("builder", C.c_int32),
+                ("ploc_radius", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class EarRecorder(C.Structure):

@@ -41,6 +41,11 @@ size_t trace_smem_bytes(int num_mats, int num_tracks, int mode, int block, int n
 
 thread_local char g_err[512] = "";
 
+// Builder of ear_scene_build_bvh when the options leave it open: PLOC
+// (measured +4..6% segments/s over the LBVH on the 20,000- and
+// 2,000,000-triangle scenes).
+constexpr int kDefaultBuilder = EAR_BVH_PLOC;
+
 ear_status fail(ear_status st, const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -275,7 +280,14 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   const float pad = opts ? opts->box_pad : -1.0f;
   const int max_leaf = opts && opts->max_leaf_size > 0 ? opts->max_leaf_size : 1;
   if (max_leaf > 16) return fail(EAR_ERR_INVALID_ARG, "max_leaf_size above 16");
-  cudaError_t e = build_lbvh(s->ds, pad, max_leaf, 0, msg, sizeof msg);
+  int builder = opts ? opts->builder : EAR_BVH_DEFAULT;
+  if (builder == EAR_BVH_DEFAULT) builder = kDefaultBuilder;
+  if (builder != EAR_BVH_LBVH && builder != EAR_BVH_PLOC)
+    return fail(EAR_ERR_INVALID_ARG, "unknown BVH builder %d", builder);
+  const int radius = opts && opts->ploc_radius > 0 ? opts->ploc_radius : 16;
+  if (radius > 256) return fail(EAR_ERR_INVALID_ARG, "ploc_radius above 256");
+  cudaError_t e = build_lbvh(s->ds, pad, max_leaf, builder == EAR_BVH_PLOC ? kBuilderPloc : kBuilderLbvh,
+                             radius, 0, msg, sizeof msg);
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,

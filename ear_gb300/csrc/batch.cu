@@ -258,11 +258,12 @@ void cache_store(const char* path, const std::string& key, const ear_batch_confi
 
 ear_status rebuild_scenes(ear_batch* b, int leaf) {
   for (ear_scene* s : b->scenes) {
-    if (s->ds.max_leaf == leaf) continue;
+    if (s->ds.max_leaf == leaf || s->ds.builder == kBuilderPloc) continue;
     ear_bvh_opts o;
     std::memset(&o, 0, sizeof o);
     o.box_pad = s->ds.box_pad;  // keep the padding the scene was built with
     o.max_leaf_size = leaf;
+    o.builder = EAR_BVH_LBVH;
     const ear_status rc = ear_scene_build_bvh(s, &o);
     if (rc != EAR_OK) return rc;
   }

@@ -8,10 +8,24 @@
 // range and split, and a bottom-up refit with one atomic visit counter per
 // node.  Compiled with --fmad=false: the per-triangle edges and normals it
 // writes must equal the CPU restatement's bit for bit.
+//
+// The alternative builder is PLOC (Meister and Bittner, "Parallel Locally-
+// Ordered Clustering for Bounding Volume Hierarchy Construction", IEEE TVCG
+// 2018): starting from the same Morton-sorted leaves, every cluster finds
+// the cluster within `radius` positions whose union box has the smallest
+// surface area; mutual nearest neighbours merge into a new node; the
+// survivors are compacted in order and the step repeats until one cluster
+// is left.  Nearest neighbours are ranked by (area, lower index, higher
+// index), a strict order in which the globally closest pair is always
+// mutual, so every step merges at least one pair.  Internal nodes are
+// numbered backwards in creation order, so the root is node 0.
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include <stdio.h>
+
+#include <utility>
 
 #include "ear_internal.h"
 
@@ -178,6 +192,105 @@ __global__ void k_refit(const float4* __restrict__ lo, const float4* __restrict_
   }
 }
 
+// ------------------------------------------------------------------ PLOC
+__device__ __forceinline__ float union_area(float4 al, float4 ah, float4 bl, float4 bh) {
+  const float dx = fmaxf(ah.x, bh.x) - fminf(al.x, bl.x);
+  const float dy = fmaxf(ah.y, bh.y) - fminf(al.y, bl.y);
+  const float dz = fmaxf(ah.z, bh.z) - fminf(al.z, bl.z);
+  return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+// Nearest neighbour of every cluster within +-radius positions; ties go
+// to the lowest index, which is the (area, min, max) order for a fixed i.
+__global__ void k_ploc_nn(const float4* __restrict__ lo, const float4* __restrict__ hi, int count,
+                          int radius, int* __restrict__ nn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float4 il = lo[i], ih = hi[i];
+  const int j0 = i - radius < 0 ? 0 : i - radius;
+  const int j1 = i + radius > count - 1 ? count - 1 : i + radius;
+  float best = 0.0f;
+  int bj = -1;
+  for (int j = j0; j <= j1; ++j) {
+    if (j == i) continue;
+    const float a = union_area(il, ih, lo[j], hi[j]);
+    if (bj < 0 || a < best) {
+      best = a;
+      bj = j;
+    }
+  }
+  nn[i] = bj;
+}
+
+__global__ void k_ploc_flags(const int* __restrict__ nn, int count, int* __restrict__ merge,
+                             int* __restrict__ keep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int j = nn[i];
+  const bool mutual = j >= 0 && nn[j] == i;
+  merge[i] = (mutual && i < j) ? 1 : 0;
+  keep[i] = (mutual && i > j) ? 0 : 1;
+}
+
+__global__ void k_ploc_totals(const int* __restrict__ merge, const int* __restrict__ mrank,
+                              const int* __restrict__ keep, const int* __restrict__ kpos, int count,
+                              int2* __restrict__ totals) {
+  totals[0] = make_int2(mrank[count - 1] + merge[count - 1], kpos[count - 1] + keep[count - 1]);
+}
+
+// Writes the merged nodes and the compacted cluster list of one step.
+__global__ void k_ploc_write(const float4* __restrict__ lo, const float4* __restrict__ hi,
+                             const int* __restrict__ id, const int* __restrict__ nn,
+                             const int* __restrict__ merge, const int* __restrict__ mrank,
+                             const int* __restrict__ keep, const int* __restrict__ kpos, int count,
+                             int node_base, float4* __restrict__ lo2, float4* __restrict__ hi2,
+                             int* __restrict__ id2, Node* __restrict__ nodes,
+                             int* __restrict__ leaf_parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count || !keep[i]) return;
+  const int p = kpos[i];
+  if (!merge[i]) {
+    lo2[p] = lo[i];
+    hi2[p] = hi[i];
+    id2[p] = id[i];
+    return;
+  }
+  const int j = nn[i];
+  const int idx = node_base - mrank[i];
+  const float4 l0 = lo[i], h0 = hi[i], l1 = lo[j], h1 = hi[j];
+  Node nd;
+  nd.a = make_float4(l0.x, h0.x, l0.y, h0.y);
+  nd.b = make_float4(l0.z, h0.z, l1.x, h1.x);
+  nd.c = make_float4(l1.y, h1.y, l1.z, h1.z);
+  nd.d = make_int4(id[i], id[j], -1, 0);
+  nodes[idx] = nd;
+  const int c[2] = {id[i], id[j]};
+  for (int k = 0; k < 2; ++k) {
+    if (c[k] >= 0) {
+      nodes[c[k]].d.z = idx;
+    } else {
+      leaf_parent[~c[k] & kLeafStartMask] = idx;
+    }
+  }
+  lo2[p] = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.0f);
+  hi2[p] = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.0f);
+  id2[p] = idx;
+}
+
+// Initial clusters: the padded leaf boxes in sorted order, leaf code ~k.
+__global__ void k_ploc_init(const float4* __restrict__ lo, const float4* __restrict__ hi,
+                            const int32_t* __restrict__ sorted_idx, int n, float pad,
+                            float4* __restrict__ clo, float4* __restrict__ chi,
+                            int* __restrict__ cid) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int t = sorted_idx[k];
+  const float4 l = lo[t], h = hi[t];
+  clo[k] = make_float4(l.x - pad, l.y - pad, l.z - pad, 0.0f);
+  chi[k] = make_float4(h.x + pad, h.y + pad, h.z + pad, 0.0f);
+  cid[k] = ~k;
+}
+
 // Leaf collapse: an internal child whose subtree spans at most max_leaf
 // triangles (a contiguous range of the sorted order) becomes one leaf over
 // that range.  Its box in the parent is already the union of the subtree.
@@ -249,8 +362,8 @@ __global__ void k_single(const float4* __restrict__ lo, const float4* __restrict
 
 }  // namespace
 
-cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t stream,
-                       char* err, size_t errlen) {
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder, int radius,
+                       cudaStream_t stream, char* err, size_t errlen) {
   const int64_t n64 = s.num_tris;
   cudaError_t rc = cudaSuccess;
   err[0] = 0;
@@ -264,6 +377,13 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t
   int32_t *idx = nullptr, *idx2 = nullptr, *leaf_parent = nullptr;
   int2* range = nullptr;
   int* dmax = nullptr;
+  // PLOC
+  float4 *clo = nullptr, *chi = nullptr, *clo2 = nullptr, *chi2 = nullptr;
+  int *cid = nullptr, *cid2 = nullptr, *nnb = nullptr, *mflag = nullptr, *mrank = nullptr;
+  int *kflag = nullptr, *kpos = nullptr;
+  int2* totals = nullptr;
+  void* stmp = nullptr;
+  size_t stmp_bytes = 0;
   void* tmp = nullptr;
   size_t tmp_bytes = 0;
   uint32_t hb[7];
@@ -331,16 +451,67 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t
     CK(cudaMalloc(&tmp, tmp_bytes));
     CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, codes, codes2, idx, idx2, n, 0, 30,
                                        stream));
-    k_karras<<<(nn + B - 1) / B, B, 0, stream>>>(codes2, n, s.nodes, leaf_parent, range);
-    CK(cudaGetLastError());
-    k_refit<<<G, B, 0, stream>>>(lo, hi, idx2, leaf_parent, n, s.box_pad, s.nodes, node_lo,
-                                 node_hi, visits);
-    CK(cudaGetLastError());
-    k_depth<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, dmax);
-    CK(cudaGetLastError());
-    if (max_leaf > 1) {
-      k_collapse<<<(nn + B - 1) / B, B, 0, stream>>>(range, n, max_leaf, s.nodes);
+    if (builder == kBuilderPloc) {
+      CK(cudaMalloc(&clo, sizeof(float4) * n));
+      CK(cudaMalloc(&chi, sizeof(float4) * n));
+      CK(cudaMalloc(&clo2, sizeof(float4) * n));
+      CK(cudaMalloc(&chi2, sizeof(float4) * n));
+      CK(cudaMalloc(&cid, sizeof(int) * n));
+      CK(cudaMalloc(&cid2, sizeof(int) * n));
+      CK(cudaMalloc(&nnb, sizeof(int) * n));
+      CK(cudaMalloc(&mflag, sizeof(int) * n));
+      CK(cudaMalloc(&mrank, sizeof(int) * n));
+      CK(cudaMalloc(&kflag, sizeof(int) * n));
+      CK(cudaMalloc(&kpos, sizeof(int) * n));
+      CK(cudaMalloc(&totals, sizeof(int2)));
+      CK(cub::DeviceScan::ExclusiveSum(nullptr, stmp_bytes, mflag, mrank, n, stream));
+      CK(cudaMalloc(&stmp, stmp_bytes));
+      k_ploc_init<<<G, B, 0, stream>>>(lo, hi, idx2, n, s.box_pad, clo, chi, cid);
       CK(cudaGetLastError());
+      int count = n, created = 0;
+      for (int step = 0; count > 1; ++step) {
+        const int g = (count + B - 1) / B;
+        k_ploc_nn<<<g, B, 0, stream>>>(clo, chi, count, radius, nnb);
+        CK(cudaGetLastError());
+        k_ploc_flags<<<g, B, 0, stream>>>(nnb, count, mflag, kflag);
+        CK(cudaGetLastError());
+        size_t tb = stmp_bytes;
+        CK(cub::DeviceScan::ExclusiveSum(stmp, tb, mflag, mrank, count, stream));
+        tb = stmp_bytes;
+        CK(cub::DeviceScan::ExclusiveSum(stmp, tb, kflag, kpos, count, stream));
+        k_ploc_totals<<<1, 1, 0, stream>>>(mflag, mrank, kflag, kpos, count, totals);
+        CK(cudaGetLastError());
+        k_ploc_write<<<g, B, 0, stream>>>(clo, chi, cid, nnb, mflag, mrank, kflag, kpos, count,
+                                          (n - 2) - created, clo2, chi2, cid2, s.nodes, leaf_parent);
+        CK(cudaGetLastError());
+        int2 tot;
+        CK(cudaMemcpyAsync(&tot, totals, sizeof tot, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (tot.x <= 0 || step > 4 * n) {
+          snprintf(err, errlen, "PLOC made no progress at %d clusters", count);
+          rc = cudaErrorUnknown;
+          goto done;
+        }
+        std::swap(clo, clo2);
+        std::swap(chi, chi2);
+        std::swap(cid, cid2);
+        count = tot.y;
+        created += tot.x;
+      }
+      k_depth<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, dmax);
+      CK(cudaGetLastError());
+    } else {
+      k_karras<<<(nn + B - 1) / B, B, 0, stream>>>(codes2, n, s.nodes, leaf_parent, range);
+      CK(cudaGetLastError());
+      k_refit<<<G, B, 0, stream>>>(lo, hi, idx2, leaf_parent, n, s.box_pad, s.nodes, node_lo,
+                                   node_hi, visits);
+      CK(cudaGetLastError());
+      k_depth<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, dmax);
+      CK(cudaGetLastError());
+      if (max_leaf > 1) {
+        k_collapse<<<(nn + B - 1) / B, B, 0, stream>>>(range, n, max_leaf, s.nodes);
+        CK(cudaGetLastError());
+      }
     }
     CK(cudaMemcpyAsync(&depth, dmax, sizeof(int), cudaMemcpyDeviceToHost, stream));
   }
@@ -349,7 +520,8 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t
   CK(cudaStreamSynchronize(stream));
   s.num_nodes = nn;
   s.max_depth = depth;
-  s.max_leaf = max_leaf;
+  s.max_leaf = builder == kBuilderPloc ? 1 : max_leaf;
+  s.builder = builder;
   if (depth > 62) {
     snprintf(err, errlen, "LBVH depth %d exceeds the 62 levels of the traversal trail", depth);
     rc = cudaErrorInvalidValue;
@@ -368,6 +540,19 @@ done:
   cudaFree(visits);
   cudaFree(range);
   cudaFree(dmax);
+  cudaFree(clo);
+  cudaFree(chi);
+  cudaFree(clo2);
+  cudaFree(chi2);
+  cudaFree(cid);
+  cudaFree(cid2);
+  cudaFree(nnb);
+  cudaFree(mflag);
+  cudaFree(mrank);
+  cudaFree(kflag);
+  cudaFree(kpos);
+  cudaFree(totals);
+  cudaFree(stmp);
   cudaFree(tmp);
   return rc;
 }

@@ -33,6 +33,7 @@ struct DeviceScene {
   int max_depth = 0;
   float box_pad = 0.0f;
   int max_leaf = 1;
+  int builder = 1;
   Node* nodes = nullptr;
   float4* tris = nullptr;
   float4* nrm = nullptr;
@@ -161,9 +162,13 @@ enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 
 // LBVH build (bvh_build.cu).  Returns a cudaError_t; `err` receives a
 // message on failure.
-// Subtrees of at most max_leaf (1..16) triangles become one leaf.
-cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, cudaStream_t stream, char* err,
-                       size_t errlen);
+// Binary BVH over the scene's triangles: builder kBuilderLbvh (Karras
+// 2012; subtrees of at most max_leaf (1..16) triangles become one leaf) or
+// kBuilderPloc (locally-ordered clustering within +-radius positions;
+// single-triangle leaves).
+enum { kBuilderLbvh = 1, kBuilderPloc = 2 };
+cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder, int radius,
+                       cudaStream_t stream, char* err, size_t errlen);
 
 // Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
 // kModeBatch traces many jobs (scene, source, recorders) from one work

@@ -182,14 +182,16 @@ __device__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slac
     float t0, t1;
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
-    if (h0 && ch.x < 0) {
-      blocked |= leaf_test<ANY>(S, ch.x, o, d, h, c, err);
-      h0 = false;
+    // the hit leaf children (0, 1 or 2) are tested by one loop, so lanes
+    // with one leaf and lanes with two share the same instructions
+    const bool l0 = h0 && ch.x < 0, l1 = h1 && ch.y < 0;
+    const int nleaf = (int)l0 + (int)l1;
+    for (int q = 0; q < nleaf; ++q) {
+      const int code = (q == 0 && l0) ? ch.x : ch.y;
+      blocked |= leaf_test<ANY>(S, code, o, d, h, c, err);
     }
-    if (h1 && ch.y < 0) {
-      blocked |= leaf_test<ANY>(S, ch.y, o, d, h, c, err);
-      h1 = false;
-    }
+    h0 = h0 && !l0;
+    h1 = h1 && !l1;
     if (ANY && blocked) break;
     if (h0 || h1) {
       if (h0 && h1) {

@@ -147,7 +147,8 @@ class Tracer:
     ear_scene_build_bvh)."""
 
     def __init__(self, vertices, material_ids, materials: Sequence[Material], device: int = 0,
-                 box_pad: float = -1.0):
+                 box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
+                 ploc_radius: int = 0):
         L = N.lib()
         self._v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
         self._m = np.ascontiguousarray(material_ids, dtype=np.int32).reshape(-1)
@@ -167,9 +168,20 @@ class Tracer:
         h = C.c_void_p()
         N.check(L.ear_scene_create(C.byref(desc), C.byref(h)))
         self._h = h
+        self.build_bvh(box_pad=box_pad, builder=builder, max_leaf=max_leaf,
+                       ploc_radius=ploc_radius)
+
+    def build_bvh(self, box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
+                  ploc_radius: int = 0) -> None:
+        """(Re)build the BVH: builder "default", "lbvh" or "ploc"."""
         opts = N.EarBvhOpts()
         opts.box_pad = float(box_pad)
-        N.check(L.ear_scene_build_bvh(self._h, C.byref(opts)))
+        opts.max_leaf_size = int(max_leaf)
+        opts.builder = {"default": N.EAR_BVH_DEFAULT, "lbvh": N.EAR_BVH_LBVH,
+                        "ploc": N.EAR_BVH_PLOC}[builder]
+        opts.ploc_radius = int(ploc_radius)
+        N.check(N.lib().ear_scene_build_bvh(self._h, C.byref(opts)))
+        self._builder = builder
 
     @property
     def num_triangles(self) -> int:
@@ -181,7 +193,8 @@ class Tracer:
         N.check(N.lib().ear_scene_info(self._h, C.byref(nt), C.byref(nn), C.byref(depth),
                                         C.byref(pad), C.byref(db)))
         return {"triangles": nt.value, "nodes": nn.value, "max_depth": depth.value,
-                "box_pad": pad.value, "device_bytes": db.value}
+                "box_pad": pad.value, "device_bytes": db.value,
+                "builder": getattr(self, "_builder", "default")}
 
     def render(self, source: Source, recorders: Sequence[Recorder], *, keyframe: int = -1,
                out=None, **kw) -> RenderResult:

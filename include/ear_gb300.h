@@ -102,8 +102,19 @@ typedef struct ear_bvh_opts {
      fewer node visits, more triangle tests per visit.  Never changes which
      triangle is reported. */
   int32_t max_leaf_size;
-  int32_t reserved[6];
+  /* EAR_BVH_DEFAULT, EAR_BVH_LBVH (Morton-order linear BVH, Karras 2012) or
+     EAR_BVH_PLOC (locally-ordered agglomerative clustering over the same
+     Morton order, Meister and Bittner 2018: a tree of lower surface-area
+     cost, single-triangle leaves).  Never changes which triangle is
+     reported. */
+  int32_t builder;
+  int32_t ploc_radius;     /* PLOC search radius in positions (0 = 16) */
+  int32_t reserved[4];
 } ear_bvh_opts;
+
+#define EAR_BVH_DEFAULT 0
+#define EAR_BVH_LBVH 1
+#define EAR_BVH_PLOC 2
 
 /* OUT1 (mono, src/MonoRecorder.cpp:38-59) or OUT2 (stereo,
  * src/StereoRecorder.cpp:33-67) block, evaluated at the keyframe being

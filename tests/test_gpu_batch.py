@@ -94,6 +94,8 @@ def test_autotuner_applies_a_schedule_and_changes_no_result(sweep, tmp_path):
     plain = _plain(tracers, jobs, render)
     kw = {k: v for k, v in render.items() if k != "num_rays"}
     cache = tmp_path / "tune.txt"
+    for t in tracers:  # leaf sizes apply to LBVH scenes
+        t.build_bvh(builder="lbvh")
     with Batch(tracers, jobs, exact=True, **kw) as b:
         res = b.tune(trial_fraction=0.5, tune_leaf_size=True, repeats=1, cache_path=str(cache))
         assert res["candidates"] >= 4 and not res["from_cache"]
@@ -106,13 +108,8 @@ def test_autotuner_applies_a_schedule_and_changes_no_result(sweep, tmp_path):
         res2 = b.tune(tune_leaf_size=True, cache_path=str(cache))
         assert res2["from_cache"] and res2["best"]["block"] == res["best"]["block"]
         _check(b, plain, b.run())
-    for t in tracers:  # back to single-triangle leaves for the other tests
-        from ear_gb300 import _native as N
-        import ctypes as C
-        o = N.EarBvhOpts()
-        o.box_pad = -1.0
-        o.max_leaf_size = 1
-        N.check(N.lib().ear_scene_build_bvh(t._h, C.byref(o)))
+    for t in tracers:  # back to the default builder for the other tests
+        t.build_bvh()
 
 
 def test_leaf_size_changes_no_hit(sweep):
@@ -122,13 +119,14 @@ def test_leaf_size_changes_no_hit(sweep):
     rooms, render, tracers, jobs = sweep
     r = rooms[-1]
     kw = dict(render, num_rays=400, context=3)
-    with Tracer(r.vertices, r.material_ids, r.materials) as t:
+    with Tracer(r.vertices, r.material_ids, r.materials, builder="lbvh") as t:
         ref = t.trace_debug(r.sources[0], r.listeners[:1], band=1, max_record=60, keyframe=0,
                             exact=True, **kw)
         for leaf in (2, 4, 16):
             o = N.EarBvhOpts()
             o.box_pad = -1.0
             o.max_leaf_size = leaf
+            o.builder = N.EAR_BVH_LBVH
             N.check(N.lib().ear_scene_build_bvh(t._h, C.byref(o)))
             got = t.trace_debug(r.sources[0], r.listeners[:1], band=1, max_record=60,
                                 keyframe=0, exact=True, **kw)
