@@ -63,15 +63,23 @@ __device__ __forceinline__ Ray make_ray(V3 o, V3 d) {
   return r;
 }
 
-// Slab test against [lo, hi] for t in [0, tmax]; conservative only.
+// Slab test against [lo, hi] for t in [0, tmax] (tmax > 0); conservative
+// only.  The entry distance tn = max(min x, min y, min z, 0) and exit
+// distance tf = min(max x, max y, max z, tmax) use 3-input integer min/max
+// on the float bit patterns: signed-integer order equals float order among
+// non-negative floats and puts every negative float below them, so the
+// relu max gives tn exactly, and tf, which is only compared with tn >= 0,
+// keeps its sign.
 __device__ __forceinline__ bool box_hit(float lx, float hx, float ly, float hy, float lz, float hz,
                                         const Ray& r, float tmax, float& tnear) {
   const float tx0 = __fmaf_rn(lx, r.ix, r.nx), tx1 = __fmaf_rn(hx, r.ix, r.nx);
   const float ty0 = __fmaf_rn(ly, r.iy, r.ny), ty1 = __fmaf_rn(hy, r.iy, r.ny);
   const float tz0 = __fmaf_rn(lz, r.iz, r.nz), tz1 = __fmaf_rn(hz, r.iz, r.nz);
-  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-  const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-  tnear = tn;
+  const int tn = __vimax3_s32_relu(__float_as_int(fminf(tx0, tx1)), __float_as_int(fminf(ty0, ty1)),
+                                   __float_as_int(fminf(tz0, tz1)));
+  const int tf = __vimin3_s32(__float_as_int(fmaxf(tx0, tx1)), __float_as_int(fmaxf(ty0, ty1)),
+                              __float_as_int(fminf(fmaxf(tz0, tz1), tmax)));
+  tnear = __int_as_float(tn);
   return tn <= tf;
 }
 
