@@ -311,6 +311,58 @@ __global__ void k_collapse(const int2* __restrict__ range, int n, int max_leaf, 
   nodes[i].d = d;
 }
 
+// ---------------------------------------------------- depth-first layout
+// Internal nodes are renumbered in depth-first preorder (a node, its child
+// 0 subtree, its child 1 subtree), so a node's first child is the next
+// 64 bytes and every subtree is one contiguous range: traversal steps that
+// descend touch neighbouring cache lines.  Subtree sizes (internal nodes)
+// come bottom-up with one atomic visit counter per node, as in the refit;
+// each node then finds its position by walking up to the root.
+__global__ void k_subtree_size(const int32_t* __restrict__ leaf_parent, int n, const Node* nodes,
+                               uint32_t* visits, int* size) {
+  const int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= n) return;
+  int p = leaf_parent[leaf];
+  while (p >= 0) {
+    __threadfence();
+    if (atomicAdd(&visits[p], 1u) == 0u) return;
+    __threadfence();
+    const int4 ch = __ldcg(&nodes[p].d);
+    const int s0 = ch.x >= 0 ? __ldcg(&size[ch.x]) : 0;
+    const int s1 = ch.y >= 0 ? __ldcg(&size[ch.y]) : 0;
+    size[p] = 1 + s0 + s1;
+    p = ch.z;
+  }
+}
+
+__global__ void k_preorder(const Node* __restrict__ nodes, const int* __restrict__ size, int nn,
+                           int* __restrict__ pos) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nn) return;
+  int p = 0, cur = v;
+  for (int guard = 0; guard < 4096; ++guard) {
+    const int par = nodes[cur].d.z;
+    if (par < 0) break;
+    const int4 pc = nodes[par].d;
+    p += (pc.x == cur) ? 1 : 1 + (pc.x >= 0 ? size[pc.x] : 0);
+    cur = par;
+  }
+  pos[v] = p;
+}
+
+__global__ void k_permute(const Node* __restrict__ nodes, const int* __restrict__ pos, int nn,
+                          Node* __restrict__ out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nn) return;
+  const int pv = pos[v];
+  if ((unsigned)pv >= (unsigned)nn) return;  // cannot happen for a valid tree
+  Node nd = nodes[v];
+  if (nd.d.x >= 0) nd.d.x = pos[nd.d.x];
+  if (nd.d.y >= 0) nd.d.y = pos[nd.d.y];
+  if (nd.d.z >= 0) nd.d.z = pos[nd.d.z];
+  out[pv] = nd;
+}
+
 // Depth of every leaf (internal nodes on its root path + 1).
 __global__ void k_depth(const int32_t* __restrict__ leaf_parent, int n, const Node* __restrict__ nodes,
                         int* max_depth) {
@@ -377,6 +429,8 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   int32_t *idx = nullptr, *idx2 = nullptr, *leaf_parent = nullptr;
   int2* range = nullptr;
   int* dmax = nullptr;
+  int *ssize = nullptr, *spos = nullptr;
+  Node* reordered = nullptr;
   // PLOC
   float4 *clo = nullptr, *chi = nullptr, *clo2 = nullptr, *chi2 = nullptr;
   int *cid = nullptr, *cid2 = nullptr, *nnb = nullptr, *mflag = nullptr, *mrank = nullptr;
@@ -514,6 +568,21 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
       }
     }
     CK(cudaMemcpyAsync(&depth, dmax, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    if (builder == kBuilderPloc || max_leaf <= 1) {
+      // depth-first layout (not after a leaf collapse, which leaves
+      // unreachable nodes behind)
+      CK(cudaMalloc(&ssize, sizeof(int) * nn));
+      CK(cudaMalloc(&spos, sizeof(int) * nn));
+      CK(cudaMalloc(&reordered, sizeof(Node) * nn));
+      CK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nn, stream));
+      k_subtree_size<<<G, B, 0, stream>>>(leaf_parent, n, s.nodes, visits, ssize);
+      CK(cudaGetLastError());
+      k_preorder<<<(nn + B - 1) / B, B, 0, stream>>>(s.nodes, ssize, nn, spos);
+      CK(cudaGetLastError());
+      k_permute<<<(nn + B - 1) / B, B, 0, stream>>>(s.nodes, spos, nn, reordered);
+      CK(cudaGetLastError());
+      std::swap(s.nodes, reordered);
+    }
   }
   k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris, s.nrm);
   CK(cudaGetLastError());
@@ -540,6 +609,9 @@ done:
   cudaFree(visits);
   cudaFree(range);
   cudaFree(dmax);
+  cudaFree(ssize);
+  cudaFree(spos);
+  cudaFree(reordered);
   cudaFree(clo);
   cudaFree(chi);
   cudaFree(clo2);
