@@ -332,7 +332,7 @@ def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_c
         if tune:
             t0 = time.perf_counter()
             t = b.tune(trial_fraction=0.05, min_trial_rays=64, tune_leaf_size=True, repeats=1,
-                       cache_path=tune_cache)
+                       cache_path=tune_cache, tune_width=True)
             t["tune_s"] = time.perf_counter() - t0
         b.run()  # capture + first replay
         torch.cuda.synchronize()
@@ -388,7 +388,7 @@ def run_ours(args):
     kw["seed"] = int(kw.get("seed", 0)) + rank
     exact = args.exact
     tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad,
-                    builder=args.builder)
+                    builder=args.builder, width=args.width)
     tracks = w.num_tracks
     out = torch.zeros((tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -455,7 +455,7 @@ def run_ours(args):
         e0.record(stream)
         for _ in range(e_steps):
             t2 = Tracer(vp, mp, w.materials, device=local, box_pad=args.box_pad,
-                        builder=args.builder)
+                        builder=args.builder, width=args.width)
             r2 = t2.render(w.source, w.recorders, out=host_out, exact=exact, **kw)
             t2.close()
             e_seg += int(r2.stats["segments"])
@@ -525,6 +525,8 @@ def main():
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--box-pad", type=float, default=-1.0)
     ap.add_argument("--builder", default="default", choices=["default", "lbvh", "ploc"])
+    ap.add_argument("--width", type=int, default=0, choices=[0, 2, 4],
+                    help="BVH traversal width (0: by scene size)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

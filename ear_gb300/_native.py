@@ -48,7 +48,7 @@ class EarSceneDesc(C.Structure):
 
 class EarBvhOpts(C.Structure):
     _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("builder", C.c_int32),
-                ("ploc_radius", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("ploc_radius", C.c_int32), ("width", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class EarRecorder(C.Structure):
@@ -92,17 +92,18 @@ class EarBatchJob(C.Structure):
 
 class EarBatchConfig(C.Structure):
     _fields_ = [("block", C.c_int32), ("blocks_per_sm", C.c_int32), ("max_leaf_size", C.c_int32),
-                ("no_graph", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("no_graph", C.c_int32), ("bvh_width", C.c_int32), ("reserved", C.c_int32 * 3)]
 
     def as_dict(self):
         return {"block": self.block, "blocks_per_sm": self.blocks_per_sm,
-                "max_leaf_size": self.max_leaf_size, "no_graph": self.no_graph}
+                "max_leaf_size": self.max_leaf_size, "no_graph": self.no_graph,
+                "bvh_width": self.bvh_width}
 
 
 class EarTuneOpts(C.Structure):
     _fields_ = [("trial_fraction", C.c_double), ("min_trial_rays", C.c_uint64),
                 ("tune_leaf_size", C.c_int32), ("repeats", C.c_int32), ("cache_path", C.c_char_p),
-                ("reserved", C.c_int32 * 4)]
+                ("tune_width", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class EarTuneResult(C.Structure):
@@ -120,6 +121,7 @@ SIGNATURES = {
     "ear_scene_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int64)]),
     "ear_scene_destroy": (None, [C.c_void_p]),
+    "ear_scene_set_bvh_width": (C.c_int, [C.c_void_p, C.c_int32]),
     "ear_num_tracks": (C.c_int32, [C.POINTER(EarRecorder), C.c_int32]),
     "ear_render": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder), C.c_int32,
                              C.POINTER(EarRenderParams), C.POINTER(EarHistograms),

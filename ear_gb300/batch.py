@@ -4,7 +4,7 @@
 source / listener pairs and keyframes is planned once, traced by one
 persistent launch that drains a device work queue, and replayed as a CUDA
 graph.  ``Batch.tune`` runs the project's autotuner over the launch
-schedule (block size, resident blocks per SM, BVH leaf size).
+schedule (block size, resident blocks per SM, BVH leaf size, tree width).
 
 Every job renders exactly what ``Tracer.render`` renders for the same
 scene, source position, recorders, seed and context.
@@ -74,14 +74,16 @@ class Batch:
         N.check(N.lib().ear_batch_get_config(self._h, C.byref(c)))
         return c.as_dict()
 
-    def set_config(self, block: int = 0, blocks_per_sm: int = 0, no_graph: bool = False) -> None:
+    def set_config(self, block: int = 0, blocks_per_sm: int = 0, no_graph: bool = False,
+                   bvh_width: int = 0) -> None:
         c = N.EarBatchConfig()
         c.block, c.blocks_per_sm, c.no_graph = int(block), int(blocks_per_sm), int(bool(no_graph))
+        c.bvh_width = int(bvh_width)
         N.check(N.lib().ear_batch_set_config(self._h, C.byref(c)))
 
     def tune(self, trial_fraction: float = 0.02, min_trial_rays: int = 256,
              tune_leaf_size: bool = False, repeats: int = 2,
-             cache_path: Optional[str] = None) -> dict:
+             cache_path: Optional[str] = None, tune_width: bool = False) -> dict:
         """Autotune the launch schedule on trial launches and apply the
         best; returns the chosen schedule and the trial timings."""
         o = N.EarTuneOpts()
@@ -90,6 +92,7 @@ class Batch:
         o.tune_leaf_size = int(bool(tune_leaf_size))
         o.repeats = int(repeats)
         o.cache_path = cache_path.encode() if cache_path else None
+        o.tune_width = int(bool(tune_width))
         r = N.EarTuneResult()
         N.check(N.lib().ear_batch_tune(self._h, C.byref(o), C.byref(r)))
         return {"best": r.best.as_dict(), "best_ms": r.best_ms, "default_ms": r.default_ms,

@@ -286,14 +286,26 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
     return fail(EAR_ERR_INVALID_ARG, "unknown BVH builder %d", builder);
   const int radius = opts && opts->ploc_radius > 0 ? opts->ploc_radius : 16;
   if (radius > 256) return fail(EAR_ERR_INVALID_ARG, "ploc_radius above 256");
+  const int width = opts ? opts->width : 0;
+  if (width != 0 && width != 2 && width != 4) return fail(EAR_ERR_INVALID_ARG, "width must be 0, 2 or 4");
   cudaError_t e = build_lbvh(s->ds, pad, max_leaf, builder == EAR_BVH_PLOC ? kBuilderPloc : kBuilderLbvh,
                              radius, 0, msg, sizeof msg);
+  s->ds.wide = width == 4 || (width == 0 && s->ds.num_tris >= kWideFrom);
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
                 "LBVH build: %s", msg[0] ? msg : cudaGetErrorString(e));
   }
   s->bvh = true;
+  return EAR_OK;
+}
+
+ear_status ear_scene_set_bvh_width(ear_scene* s, int32_t width) {
+  g_err[0] = 0;
+  if (!s) return fail(EAR_ERR_INVALID_ARG, "null scene");
+  if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
+  if (width != 2 && width != 4) return fail(EAR_ERR_INVALID_ARG, "width must be 2 or 4");
+  s->ds.wide = width == 4;
   return EAR_OK;
 }
 
@@ -305,7 +317,8 @@ ear_status ear_scene_info(const ear_scene* s, int64_t* num_triangles, int64_t* n
   if (max_depth) *max_depth = s->ds.max_depth;
   if (box_pad) *box_pad = s->ds.box_pad;
   if (device_bytes)
-    *device_bytes = (int64_t)(s->ds.num_nodes * sizeof(Node) + s->ds.num_tris * (48 + 16 + 36 + 4));
+    *device_bytes = (int64_t)(s->ds.num_nodes * sizeof(Node) + s->ds.num_nodes4 * sizeof(Node4) +
+                              s->ds.num_tris * (48 + 16 + 36 + 4));
   return EAR_OK;
 }
 
@@ -313,6 +326,7 @@ void ear_scene_destroy(ear_scene* s) {
   if (!s) return;
   cudaSetDevice(s->device);
   cudaFree(s->ds.nodes);
+  cudaFree(s->ds.nodes4);
   cudaFree(s->ds.tris);
   cudaFree(s->ds.nrm);
   cudaFree(s->ds.vertices);
@@ -364,10 +378,12 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   const bool exact = (p->flags & EAR_FLAG_EXACT) != 0;
   out->ops = exact ? &kTraceExact : &kTraceFast;
   a.nodes = s->ds.nodes;
+  a.nodes4 = s->ds.nodes4;
+  a.wide = s->ds.wide;
   a.tris = s->ds.tris;
   a.nrm = s->ds.nrm;
   a.num_tris = (int)s->ds.num_tris;
-  a.num_nodes = (int)s->ds.num_nodes;
+  a.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   a.mats = s->mats;
   a.num_mats = s->num_mats;
   a.num_recs = nrec;
@@ -389,7 +405,7 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   a.num_bins = p->num_bins;
   a.stride = (p->num_bins + 3) & ~3;
   a.num_tracks = tracks;
-  a.traverse_budget = traverse_budget(s->ds.num_nodes);
+  a.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
   a.dbg_band = -1;
   out->num_tracks = tracks;
 
@@ -923,10 +939,12 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   std::memset(&a, 0, sizeof a);
   const TraceOps* ops = (p->flags & EAR_FLAG_EXACT) ? &kTraceExact : &kTraceFast;
   a.nodes = s->ds.nodes;
+  a.nodes4 = s->ds.nodes4;
+  a.wide = s->ds.wide;
   a.tris = s->ds.tris;
   a.nrm = s->ds.nrm;
   a.num_tris = (int)s->ds.num_tris;
-  a.num_nodes = (int)s->ds.num_nodes;
+  a.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   a.mats = s->mats;
   a.num_mats = s->num_mats;
   a.num_recs = nrec;
@@ -956,7 +974,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.direct_vis = direct ? reinterpret_cast<int*>(scratch + kNaVis) : nullptr;
   a.counters = reinterpret_cast<unsigned long long*>(scratch + kNaCounters);
   a.error_flag = reinterpret_cast<int*>(scratch + kNaError);
-  a.traverse_budget = traverse_budget(s->ds.num_nodes);
+  a.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
   a.dbg_band = -1;
 
   cudaStream_t st = (cudaStream_t)p->stream;

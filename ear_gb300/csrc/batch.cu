@@ -85,15 +85,18 @@ void free_graph(ear_batch* b) {
 
 SceneRef scene_ref(const ear_scene* s, int mat_base) {
   SceneRef r;
-  r.nodes = s->ds.nodes;
+  r.nodes2 = s->ds.nodes;
+  r.nodes4 = s->ds.nodes4;
+  r.wide = s->ds.wide;
+  r.pad = 0;
   r.tris = s->ds.tris;
   r.nrm = s->ds.nrm;
   r.num_tris = (int)s->ds.num_tris;
-  r.num_nodes = (int)s->ds.num_nodes;
+  r.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   r.box_pad = s->ds.box_pad;
   r.mat_base = mat_base;
   r.num_mats = s->num_mats;
-  r.traverse_budget = traverse_budget(s->ds.num_nodes);
+  r.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
   return r;
 }
 
@@ -214,7 +217,7 @@ ear_status trial(ear_batch* b, const ear_batch_config& c, uint64_t trial_items, 
   return EAR_OK;
 }
 
-std::string tune_key(const ear_batch* b, bool leaf) {
+std::string tune_key(const ear_batch* b, bool leaf, bool width) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, b->device);
   uint64_t tris = 0, rays = 0;
@@ -226,7 +229,8 @@ std::string tune_key(const ear_batch* b, bool leaf) {
   k << "sm" << prop.major << prop.minor << "x" << b->sm_count << ":scenes" << b->scenes.size()
     << ":jobs" << lg((uint64_t)b->jobs.size()) << ":tris" << lg(tris) << ":rays" << lg(rays)
     << ":mats" << b->total_mats << ":rec" << b->recs.size() << ":bands" << b->params.bands_mask
-    << ":exact" << ((b->params.flags & EAR_FLAG_EXACT) ? 1 : 0) << ":leaf" << (leaf ? 1 : 0);
+    << ":exact" << ((b->params.flags & EAR_FLAG_EXACT) ? 1 : 0) << ":leaf" << (leaf ? 1 : 0)
+    << ":width" << (width ? 1 : 0);
   return k.str();
 }
 
@@ -240,7 +244,7 @@ bool cache_lookup(const char* path, const std::string& key, ear_batch_config* c,
     std::string k;
     ear_batch_config t{};
     float m = 0.0f;
-    if (ls >> k >> t.block >> t.blocks_per_sm >> t.max_leaf_size >> m && k == key) {
+    if (ls >> k >> t.block >> t.blocks_per_sm >> t.max_leaf_size >> t.bvh_width >> m && k == key) {
       *c = t;
       *ms = m;
       found = true;  // the last entry for a key wins
@@ -252,8 +256,16 @@ bool cache_lookup(const char* path, const std::string& key, ear_batch_config* c,
 void cache_store(const char* path, const std::string& key, const ear_batch_config& c, float ms) {
   if (!path) return;
   std::ofstream out(path, std::ios::app);
-  out << key << " " << c.block << " " << c.blocks_per_sm << " " << c.max_leaf_size << " " << ms
-      << "\n";
+  out << key << " " << c.block << " " << c.blocks_per_sm << " " << c.max_leaf_size << " "
+      << c.bvh_width << " " << ms << "\n";
+}
+
+ear_status set_width(ear_batch* b, int width) {
+  for (ear_scene* s : b->scenes) {
+    const ear_status rc = ear_scene_set_bvh_width(s, width);
+    if (rc != EAR_OK) return rc;
+  }
+  return sync_scenes(b);
 }
 
 ear_status rebuild_scenes(ear_batch* b, int leaf) {
@@ -425,6 +437,12 @@ ear_status ear_batch_set_config(ear_batch* b, const ear_batch_config* c) {
   if (!b || !c) return fail(EAR_ERR_INVALID_ARG, "null argument");
   ear_batch_config n = *c;
   n.max_leaf_size = b->cfg.max_leaf_size;
+  if (n.bvh_width != 0 && n.bvh_width != 2 && n.bvh_width != 4)
+    return fail(EAR_ERR_INVALID_ARG, "bvh_width must be 0, 2 or 4");
+  if (n.bvh_width) {
+    const ear_status rc = set_width(b, n.bvh_width);
+    if (rc != EAR_OK) return rc;
+  }
   Schedule sc;
   const ear_status rc = schedule(b, n, &sc);
   if (rc != EAR_OK) return rc;
@@ -593,7 +611,7 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
   CU(cudaSetDevice(b->device));
   ear_tune_result res;
   std::memset(&res, 0, sizeof res);
-  const std::string key = tune_key(b, o.tune_leaf_size != 0);
+  const std::string key = tune_key(b, o.tune_leaf_size != 0, o.tune_width != 0);
   ear_batch_config cached{};
   float cached_ms = 0.0f;
   if (cache_lookup(o.cache_path, key, &cached, &cached_ms)) {
@@ -601,6 +619,11 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
       const ear_status rc = rebuild_scenes(b, cached.max_leaf_size);
       if (rc != EAR_OK) return rc;
       b->cfg.max_leaf_size = cached.max_leaf_size;
+    }
+    if (o.tune_width && (cached.bvh_width == 2 || cached.bvh_width == 4)) {
+      const ear_status rc = set_width(b, cached.bvh_width);
+      if (rc != EAR_OK) return rc;
+      b->cfg.bvh_width = cached.bvh_width;
     }
     ear_batch_config c = cached;
     c.no_graph = b->cfg.no_graph;
@@ -631,14 +654,21 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
   std::vector<int> leaves = {b->cfg.max_leaf_size > 0 ? b->cfg.max_leaf_size : 1};
   if (o.tune_leaf_size) leaves = {1, 2, 4};
   const int blocks[] = {128, 256};
+  std::vector<int> widths = {0};
+  if (o.tune_width) widths = {2, 4};
   ear_batch_config best{};
   float best_ms = 0.0f;
   bool have = false;
-  for (int leaf : leaves) {
+  for (int leaf : leaves)
+  for (int width : widths) {
     if (o.tune_leaf_size) {
       const ear_status rc = rebuild_scenes(b, leaf);
       if (rc != EAR_OK) return rc;
       b->cfg.max_leaf_size = leaf;
+    }
+    if (width) {
+      const ear_status rc = set_width(b, width);
+      if (rc != EAR_OK) return rc;
     }
     for (int block : blocks) {
       ear_batch_config probe{};
@@ -656,6 +686,7 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
         c.block = block;
         c.blocks_per_sm = q;
         c.max_leaf_size = leaf;
+        c.bvh_width = width;
         float ms = 0.0f, best_here = 0.0f;
         // one untimed warm-up, then the best of `repeats`
         rc = trial(b, c, items, &ms);
@@ -666,7 +697,8 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
           best_here = r == 0 ? ms : std::min(best_here, ms);
         }
         ++res.candidates;
-        if (leaf == leaves[0] && block == b->ops->block && q == max_per_sm) res.default_ms = best_here;
+        if (leaf == leaves[0] && width == widths[0] && block == b->ops->block && q == max_per_sm)
+          res.default_ms = best_here;
         if (!have || best_here < best_ms) {
           best = c;
           best_ms = best_here;
@@ -679,6 +711,10 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
     const ear_status rc = rebuild_scenes(b, best.max_leaf_size);
     if (rc != EAR_OK) return rc;
     b->cfg.max_leaf_size = best.max_leaf_size;
+  }
+  if (o.tune_width) {
+    const ear_status rc = set_width(b, best.bvh_width);
+    if (rc != EAR_OK) return rc;
   }
   best.no_graph = b->cfg.no_graph;
   const ear_status rc = ear_batch_set_config(b, &best);

@@ -363,6 +363,73 @@ __global__ void k_permute(const Node* __restrict__ nodes, const int* __restrict_
   out[pv] = nd;
 }
 
+// ------------------------------------------------------------- 4-wide
+// The binary nodes at even depth become 4-wide nodes whose children are the
+// binary grandchildren (or leaf children) of their subtree, in binary
+// order; their indices follow the binary order through a prefix sum, so
+// the depth-first layout carries over and the root stays node 0.
+__global__ void k_node_depth(const Node* __restrict__ nodes, int nn, int* __restrict__ depth,
+                             int* __restrict__ even) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nn) return;
+  int d = 0;
+  for (int cur = v; d < 4096; ++d) {
+    const int par = nodes[cur].d.z;
+    if (par < 0) break;
+    cur = par;
+  }
+  depth[v] = d;
+  even[v] = (d & 1) ? 0 : 1;
+}
+
+__global__ void k_build4(const Node* __restrict__ nodes, int nn, const int* __restrict__ depth,
+                         const int* __restrict__ idx4, Node4* __restrict__ out,
+                         int* __restrict__ max_depth4) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nn || (depth[v] & 1)) return;
+  const Node P = nodes[v];
+  float lx[4] = {0, 0, 0, 0}, hx[4] = {0, 0, 0, 0}, ly[4] = {0, 0, 0, 0}, hy[4] = {0, 0, 0, 0};
+  float lz[4] = {0, 0, 0, 0}, hz[4] = {0, 0, 0, 0};
+  int ch[4] = {0, 0, 0, 0};
+  int k = 0;
+  for (int c = 0; c < 2; ++c) {
+    const int cc = c == 0 ? P.d.x : P.d.y;
+    if (c == 1 && cc == P.d.x && cc < 0) break;  // the single-triangle root
+    // box of binary child c, as stored in P
+    const float bx0 = c ? P.b.z : P.a.x, bx1 = c ? P.b.w : P.a.y;
+    const float by0 = c ? P.c.x : P.a.z, by1 = c ? P.c.y : P.a.w;
+    const float bz0 = c ? P.c.z : P.b.x, bz1 = c ? P.c.w : P.b.y;
+    if (cc < 0) {
+      lx[k] = bx0; hx[k] = bx1; ly[k] = by0; hy[k] = by1; lz[k] = bz0; hz[k] = bz1;
+      ch[k] = cc;
+      ++k;
+      continue;
+    }
+    const Node C = nodes[cc];
+    for (int g = 0; g < 2; ++g) {
+      const int gg = g == 0 ? C.d.x : C.d.y;
+      lx[k] = g ? C.b.z : C.a.x; hx[k] = g ? C.b.w : C.a.y;
+      ly[k] = g ? C.c.x : C.a.z; hy[k] = g ? C.c.y : C.a.w;
+      lz[k] = g ? C.c.z : C.b.x; hz[k] = g ? C.c.w : C.b.y;
+      ch[k] = gg < 0 ? gg : idx4[gg];
+      ++k;
+    }
+  }
+  Node4 n4;
+  n4.lox = make_float4(lx[0], lx[1], lx[2], lx[3]);
+  n4.hix = make_float4(hx[0], hx[1], hx[2], hx[3]);
+  n4.loy = make_float4(ly[0], ly[1], ly[2], ly[3]);
+  n4.hiy = make_float4(hy[0], hy[1], hy[2], hy[3]);
+  n4.loz = make_float4(lz[0], lz[1], lz[2], lz[3]);
+  n4.hiz = make_float4(hz[0], hz[1], hz[2], hz[3]);
+  n4.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
+  int parent4 = -1;
+  if (P.d.z >= 0) parent4 = idx4[nodes[P.d.z].d.z];  // the binary grandparent
+  n4.meta = make_int4(parent4, (1 << k) - 1, 0, 0);
+  out[idx4[v]] = n4;
+  atomicMax(max_depth4, depth[v] / 2 + 1);
+}
+
 // Depth of every leaf (internal nodes on its root path + 1).
 __global__ void k_depth(const int32_t* __restrict__ leaf_parent, int n, const Node* __restrict__ nodes,
                         int* max_depth) {
@@ -431,6 +498,9 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   int* dmax = nullptr;
   int *ssize = nullptr, *spos = nullptr;
   Node* reordered = nullptr;
+  int *ndepth = nullptr, *even = nullptr, *idx4 = nullptr, *dmax4 = nullptr;
+  void* stmp4 = nullptr;
+  size_t stmp4_bytes = 0;
   // PLOC
   float4 *clo = nullptr, *chi = nullptr, *clo2 = nullptr, *chi2 = nullptr;
   int *cid = nullptr, *cid2 = nullptr, *nnb = nullptr, *mflag = nullptr, *mrank = nullptr;
@@ -447,6 +517,10 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   int depth = 1;
 
   if (s.nodes) cudaFree(s.nodes);
+  if (s.nodes4) cudaFree(s.nodes4);
+  s.nodes4 = nullptr;
+  s.num_nodes4 = 0;
+  s.depth4 = 0;
   if (s.tris) cudaFree(s.tris);
   if (s.nrm) cudaFree(s.nrm);
   s.nodes = nullptr;
@@ -584,6 +658,38 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
       std::swap(s.nodes, reordered);
     }
   }
+  {
+    // the 4-wide tree
+    const int gn = (nn + B - 1) / B;
+    int last_even = 0, last_idx = 0, depth4 = 0;
+    CK(cudaMalloc(&ndepth, sizeof(int) * nn));
+    CK(cudaMalloc(&even, sizeof(int) * nn));
+    CK(cudaMalloc(&idx4, sizeof(int) * nn));
+    CK(cudaMalloc(&dmax4, sizeof(int)));
+    CK(cudaMemsetAsync(dmax4, 0, sizeof(int), stream));
+    k_node_depth<<<gn, B, 0, stream>>>(s.nodes, nn, ndepth, even);
+    CK(cudaGetLastError());
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, stmp4_bytes, even, idx4, nn, stream));
+    CK(cudaMalloc(&stmp4, stmp4_bytes));
+    CK(cub::DeviceScan::ExclusiveSum(stmp4, stmp4_bytes, even, idx4, nn, stream));
+    CK(cudaMemcpyAsync(&last_even, even + nn - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&last_idx, idx4 + nn - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const int n4 = last_idx + last_even;
+    CK(cudaMalloc(&s.nodes4, sizeof(Node4) * (size_t)n4));
+    k_build4<<<gn, B, 0, stream>>>(s.nodes, nn, ndepth, idx4, s.nodes4, dmax4);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&depth4, dmax4, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    s.num_nodes4 = n4;
+    s.depth4 = depth4;
+    if (depth4 > kMaxDepth4) {
+      snprintf(err, errlen, "4-wide BVH depth %d exceeds the %d levels of the traversal trail",
+               depth4, kMaxDepth4);
+      rc = cudaErrorInvalidValue;
+      goto done;
+    }
+  }
   k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris, s.nrm);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(stream));
@@ -612,6 +718,11 @@ done:
   cudaFree(ssize);
   cudaFree(spos);
   cudaFree(reordered);
+  cudaFree(ndepth);
+  cudaFree(even);
+  cudaFree(idx4);
+  cudaFree(dmax4);
+  cudaFree(stmp4);
   cudaFree(clo);
   cudaFree(chi);
   cudaFree(clo2);

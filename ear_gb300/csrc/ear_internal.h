@@ -19,6 +19,17 @@ struct __align__(16) Node {
   int4 d;    // child0 child1 parent depth
 };
 
+// 4-wide node, 128 bytes, built from the binary tree: the binary nodes at
+// even depth, each with the up to four grandchildren (or leaf children) of
+// its subtree as children.  Boxes per axis for the four slots; a child >= 0
+// is an internal Node4, < 0 a leaf code as in Node.
+struct __align__(16) Node4 {
+  float4 lox, hix, loy, hiy, loz, hiz;
+  int4 child;
+  int4 meta;  // x: parent Node4 (-1 at the root), y: mask of occupied slots
+};
+constexpr int kMaxDepth4 = 32;  // levels of the 128-bit traversal trail
+
 constexpr int kLeafCountShift = 27;
 constexpr int kLeafStartMask = (1 << kLeafCountShift) - 1;
 
@@ -34,7 +45,11 @@ struct DeviceScene {
   float box_pad = 0.0f;
   int max_leaf = 1;
   int builder = 1;
+  int wide = 0;  // traverse the 4-wide tree
   Node* nodes = nullptr;
+  Node4* nodes4 = nullptr;
+  int64_t num_nodes4 = 0;
+  int depth4 = 0;
   float4* tris = nullptr;
   float4* nrm = nullptr;
   // inputs kept on the device in file order
@@ -67,15 +82,18 @@ struct DevRecorder {
 // One scene as the trace kernel addresses it.  A batch keeps a table of
 // these in shared memory; a single render builds one from its TraceArgs.
 struct __align__(16) SceneRef {
-  const Node* nodes;
+  const Node* nodes2;   // binary tree
+  const Node4* nodes4;  // 4-wide tree
   const float4* tris;
   const float4* nrm;
   int num_tris;
-  int num_nodes;
+  int num_nodes;  // nodes of the tree in use
   float box_pad;
   int mat_base;  // first material of the scene in the launch's table
   int num_mats;
   int traverse_budget;
+  int wide;  // 1: traverse nodes4, 0: nodes2
+  int pad;
 };
 
 // One (scene, source position, recorder set) of a batch.  Its work items
@@ -95,6 +113,8 @@ struct BatchJob {
 // Everything one trace launch needs, passed by value (param space).
 struct TraceArgs {
   const Node* nodes;
+  const Node4* nodes4;
+  int wide;
   const float4* tris;
   const float4* nrm;
   int num_tris;

@@ -76,9 +76,17 @@ inline float ray_amount(uint64_t num_rays) {
   return num_rays <= 16777216ull ? (float)num_rays : 16777216.0f;
 }
 
-inline int traverse_budget(int64_t num_nodes) {
-  return (int)std::min<int64_t>(4 * num_nodes + 64, (int64_t)1 << 30);
+// Iteration budget of one traversal.  Binary tree: every node is visited
+// once and climbed through at most twice.  4-wide tree: visited once,
+// re-entered at most three times, climbed through at most four times.
+inline int traverse_budget(int64_t num_nodes, bool wide) {
+  return (int)std::min<int64_t>((wide ? 8 : 4) * num_nodes + 64, (int64_t)1 << 30);
 }
+
+// Triangle count from which a scene traverses its 4-wide tree by default
+// (measured: +21% segments/s at 2,000,000 triangles, +2.5% at 20,000;
+// -36% at 12, where the cheaper binary visits win).
+constexpr int64_t kWideFrom = 4096;
 
 void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel_ms,
                 ear_render_stats* stats);

@@ -159,12 +159,20 @@ __device__ __forceinline__ bool leaf_test(const SceneRef& S, int code, V3 o, V3 
   return blocked;
 }
 
-// Stackless traversal.  Closest hit (ANY = false): h receives the hit.
+__device__ __forceinline__ float lane4(const float4& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ int lane4(const int4& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+// Stackless traversal of the binary tree.  Closest hit (ANY = false): h
+// receives the hit.
 // Any hit (ANY = true): returns true when blocked.  `slack` widens the
 // t-range culling so rounding in the slab test never removes a candidate.
 template <bool ANY>
-__device__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slack, Hit& h,
-                         LaneCounters& c, int& err) {
+__device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float slack, Hit& h,
+                          LaneCounters& c, int& err) {
   h.t = tlimit;
   h.pos = -1;
   h.orig = INT_MAX;
@@ -173,7 +181,7 @@ __device__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slac
   int cur = 0;
   unsigned long long trail = 1ull;
   int iters = 0;
-  const Node* __restrict__ nodes = S.nodes;
+  const Node* __restrict__ nodes = S.nodes2;
   bool blocked = false;
   const int err0 = err;
   for (;;) {
@@ -240,6 +248,141 @@ __device__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slac
     return false;
   }
   return blocked;
+}
+
+// Stackless traversal of the 4-wide tree.  Closest hit (ANY = false): h
+// receives the hit.  Any hit (ANY = true): returns true when blocked.
+// `slack` widens the t-range culling so rounding in the slab test never
+// removes a candidate.
+//
+// The trail holds, per level of the current root path, a 4-bit mask of the
+// node's hit children not yet visited (newest level in the low nibble,
+// 128 bits for 32 levels).  A node visit tests its candidate slots' boxes,
+// tests hit leaf children at once (one merged loop) and descends into the
+// nearest hit internal child, pushing the others.  At a dead end the walk
+// climbs parent links to the deepest level with pending children and
+// re-enters that node, re-testing only the pending slots against the
+// current limit (after Afra and Szirmay-Kalos, "Stackless multi-BVH
+// traversal for CPU, MIC and GPU ray tracing", CGF 2014).  The closest hit
+// is the lexicographic (t, index) minimum and the any-hit result a
+// boolean, so neither depends on the visiting order.
+template <bool ANY>
+__device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float slack, Hit& h,
+                          LaneCounters& c, int& err) {
+  h.t = tlimit;
+  h.pos = -1;
+  h.orig = INT_MAX;
+  if (S.num_tris == 0) return false;
+  const Ray r = make_ray(o, d);
+  const Node4* __restrict__ nodes = S.nodes4;
+  int cur = 0;
+  unsigned long long tlo = 0ull, thi = 0ull;  // the trail
+  int depth = 0;                              // nibbles on the trail
+  bool reentry = false;  // cur's own pending mask is the low nibble
+  int iters = 0;
+  bool blocked = false;
+  const int err0 = err;
+  for (;;) {
+    if (++iters > S.traverse_budget) {
+      err |= kErrBudget;
+      break;
+    }
+    cur = clamp_index(cur, S.num_nodes, err);
+    const Node4* nd = nodes + cur;
+    c.nodes += 2;  // two 64-byte halves
+    const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy);
+    const float4 hy = __ldg(&nd->hiy), lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+    const int4 ch = __ldg(&nd->child), meta = __ldg(&nd->meta);
+    const unsigned cand = (reentry ? (unsigned)(tlo & 0xFull) : 0xFu) & (unsigned)meta.y;
+    const float lim = ANY ? tlimit + slack : h.t + (h.t * 2.44140625e-4f + slack);
+    unsigned hit = 0u, leaf = 0u;
+    float tk[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float tn;
+      const bool b = box_hit(lane4(lx, k), lane4(hx, k), lane4(ly, k), lane4(hy, k), lane4(lz, k),
+                             lane4(hz, k), r, lim, tn);
+      tk[k] = tn;
+      if (((cand >> k) & 1u) && b) hit |= 1u << k;
+      if (lane4(ch, k) < 0) leaf |= 1u << k;
+    }
+    // hit leaf children, one merged loop
+    for (unsigned lm = hit & leaf; lm; lm &= lm - 1u) {
+      const int k = __ffs(lm) - 1;
+      blocked |= leaf_test<ANY>(S, lane4(ch, k), o, d, h, c, err);
+    }
+    if (ANY && blocked) break;
+    hit &= ~leaf;
+    if (hit) {
+      int kb = -1;
+      float best = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (((hit >> k) & 1u) && (kb < 0 || tk[k] < best)) {
+          best = tk[k];
+          kb = k;
+        }
+      const unsigned rest = hit & ~(1u << kb);
+      if (reentry) {
+        tlo = (tlo & ~0xFull) | rest;
+      } else {
+        thi = (thi << 4) | (tlo >> 60);
+        tlo = (tlo << 4) | rest;
+        ++depth;
+      }
+      cur = lane4(ch, kb);
+      reentry = false;
+      continue;
+    }
+    // dead end: climb to the deepest level with pending children
+    if (reentry) {  // cur's own pending mask is exhausted
+      tlo = (tlo >> 4) | (thi << 60);
+      thi >>= 4;
+      --depth;
+    }
+    int par = meta.x;
+    bool done = false;
+    for (;;) {
+      if (depth == 0) {
+        done = true;
+        break;
+      }
+      if (tlo & 0xFull) {
+        cur = par;
+        reentry = true;
+        break;
+      }
+      tlo = (tlo >> 4) | (thi << 60);
+      thi >>= 4;
+      --depth;
+      cur = clamp_index(par, S.num_nodes, err);
+      if (depth == 0) {
+        done = true;
+        break;
+      }
+      if (++iters > S.traverse_budget) {
+        err |= kErrBudget;
+        done = true;
+        break;
+      }
+      par = __ldg(&nodes[cur].meta.x);
+    }
+    if (done) break;
+  }
+  if (err != err0) {
+    h.pos = -1;
+    return false;
+  }
+  return blocked;
+}
+
+// The scene's tree: 4-wide for large scenes (fewer dependent node loads
+// per query), binary for small ones (cheaper visits).
+template <bool ANY>
+__device__ __forceinline__ bool traverse(const SceneRef& S, V3 o, V3 d, float tlimit, float slack,
+                                         Hit& h, LaneCounters& c, int& err) {
+  return S.wide ? traverse4<ANY>(S, o, d, tlimit, slack, h, c, err)
+                : traverse2<ANY>(S, o, d, tlimit, slack, h, c, err);
 }
 
 // ------------------------------------------------------------- sampling
@@ -374,7 +517,9 @@ __device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef*
                                              const PathState& st) {
   if (MODE == kModeBatch) return s_scenes[st.scene];
   SceneRef S;
-  S.nodes = a.nodes;
+  S.nodes2 = a.nodes;
+  S.nodes4 = a.nodes4;
+  S.wide = a.wide;
   S.tris = a.tris;
   S.nrm = a.nrm;
   S.num_tris = a.num_tris;

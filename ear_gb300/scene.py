@@ -148,7 +148,7 @@ class Tracer:
 
     def __init__(self, vertices, material_ids, materials: Sequence[Material], device: int = 0,
                  box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
-                 ploc_radius: int = 0):
+                 ploc_radius: int = 0, width: int = 0):
         L = N.lib()
         self._v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
         self._m = np.ascontiguousarray(material_ids, dtype=np.int32).reshape(-1)
@@ -169,18 +169,21 @@ class Tracer:
         N.check(L.ear_scene_create(C.byref(desc), C.byref(h)))
         self._h = h
         self.build_bvh(box_pad=box_pad, builder=builder, max_leaf=max_leaf,
-                       ploc_radius=ploc_radius)
+                       ploc_radius=ploc_radius, width=width)
 
     def build_bvh(self, box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
-                  ploc_radius: int = 0) -> None:
-        """(Re)build the BVH: builder "default", "lbvh" or "ploc"."""
+                  ploc_radius: int = 0, width: int = 0) -> None:
+        """(Re)build the BVH: builder "default", "lbvh" or "ploc"; traversal
+        width 2, 4 or 0 (4-wide from 4096 triangles)."""
         opts = N.EarBvhOpts()
         opts.box_pad = float(box_pad)
         opts.max_leaf_size = int(max_leaf)
         opts.builder = {"default": N.EAR_BVH_DEFAULT, "lbvh": N.EAR_BVH_LBVH,
                         "ploc": N.EAR_BVH_PLOC}[builder]
         opts.ploc_radius = int(ploc_radius)
+        opts.width = int(width)
         N.check(N.lib().ear_scene_build_bvh(self._h, C.byref(opts)))
+        self._width = int(width) if width else (4 if self.num_triangles >= 4096 else 2)
         self._builder = builder
 
     @property
@@ -194,7 +197,13 @@ class Tracer:
                                         C.byref(pad), C.byref(db)))
         return {"triangles": nt.value, "nodes": nn.value, "max_depth": depth.value,
                 "box_pad": pad.value, "device_bytes": db.value,
-                "builder": getattr(self, "_builder", "default")}
+                "builder": getattr(self, "_builder", "default"),
+                "width": getattr(self, "_width", 2)}
+
+    def set_width(self, width: int) -> None:
+        """Traverse the binary (2) or 4-wide (4) tree; no rebuild."""
+        N.check(N.lib().ear_scene_set_bvh_width(self._h, int(width)))
+        self._width = int(width)
 
     def render(self, source: Source, recorders: Sequence[Recorder], *, keyframe: int = -1,
                out=None, **kw) -> RenderResult:

@@ -109,7 +109,12 @@ typedef struct ear_bvh_opts {
      reported. */
   int32_t builder;
   int32_t ploc_radius;     /* PLOC search radius in positions (0 = 16) */
-  int32_t reserved[4];
+  /* Tree the traversal uses: 2 (binary), 4 (4-wide, built from the binary
+     tree: fewer dependent node loads per query, costlier visits) or 0 =
+     4-wide from 4096 triangles on.  Both trees are built; the choice can
+     be changed later with ear_scene_set_bvh_width.  Never changes a result. */
+  int32_t width;
+  int32_t reserved[3];
 } ear_bvh_opts;
 
 #define EAR_BVH_DEFAULT 0
@@ -152,6 +157,10 @@ typedef struct ear_render_params {
   int32_t reserved0;
   void* stream;            /* cudaStream_t, NULL = default stream */
 } ear_render_params;
+
+/* Selects the tree the traversal uses (2 or 4, see ear_bvh_opts.width)
+   without rebuilding.  No counterpart in the reference. */
+ear_status ear_scene_set_bvh_width(ear_scene* scene, int32_t width);
 
 /* Per-render statistics (counted on the device). */
 typedef struct ear_render_stats {
@@ -285,7 +294,9 @@ typedef struct ear_batch_config {
                              set by ear_batch_tune (read-only otherwise) */
   int32_t no_graph;       /* 1: launch directly instead of replaying the
                              captured CUDA graph */
-  int32_t reserved[4];
+  int32_t bvh_width;      /* tree width the batch's scenes traverse (2 or 4);
+                             set by ear_batch_tune, 0 = the scenes' own */
+  int32_t reserved[3];
 } ear_batch_config;
 
 /* Plans a batch: validates the jobs, derives the recorder constants,
@@ -325,7 +336,8 @@ ear_status ear_render_batch(ear_scene* const* scenes, int32_t num_scenes,
 /* Autotuner.  Times trial launches of the batch -- every job with a
    fraction of its rays -- over the schedule space (block size x blocks per
    SM, and with tune_leaf_size the BVH leaf size, which rebuilds the
-   batch's scenes) and applies the fastest.  With cache_path, results are
+   batch's scenes; with tune_width the binary or 4-wide tree) and applies
+   the fastest.  With cache_path, results are
    kept in that text file under a key of the device and the batch's shape
    and are reused without timing. */
 typedef struct ear_tune_opts {
@@ -334,7 +346,8 @@ typedef struct ear_tune_opts {
   int32_t tune_leaf_size;  /* 1: also try leaf sizes 1, 2, 4 */
   int32_t repeats;         /* timed runs per candidate, best kept (0 = 2) */
   const char* cache_path;  /* NULL: no persistent cache */
-  int32_t reserved[4];
+  int32_t tune_width;      /* 1: also try binary and 4-wide traversal */
+  int32_t reserved[3];
 } ear_tune_opts;
 
 typedef struct ear_tune_result {

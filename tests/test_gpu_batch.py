@@ -97,18 +97,21 @@ def test_autotuner_applies_a_schedule_and_changes_no_result(sweep, tmp_path):
     for t in tracers:  # leaf sizes apply to LBVH scenes
         t.build_bvh(builder="lbvh")
     with Batch(tracers, jobs, exact=True, **kw) as b:
-        res = b.tune(trial_fraction=0.5, tune_leaf_size=True, repeats=1, cache_path=str(cache))
-        assert res["candidates"] >= 4 and not res["from_cache"]
+        res = b.tune(trial_fraction=0.5, tune_leaf_size=True, repeats=1, cache_path=str(cache),
+                     tune_width=True)
+        assert res["candidates"] >= 8 and not res["from_cache"]
         assert res["best_ms"] > 0 and res["default_ms"] > 0
         cfg = b.config
         assert cfg["max_leaf_size"] in (1, 2, 4) and cfg["block"] in (128, 256)
+        assert cfg["bvh_width"] in (2, 4)
         _check(b, plain, b.run())
     # a second batch of the same shape takes the cached schedule
     with Batch(tracers, jobs, exact=True, **kw) as b:
-        res2 = b.tune(tune_leaf_size=True, cache_path=str(cache))
+        res2 = b.tune(tune_leaf_size=True, cache_path=str(cache), tune_width=True)
         assert res2["from_cache"] and res2["best"]["block"] == res["best"]["block"]
+        assert res2["best"]["bvh_width"] == res["best"]["bvh_width"]
         _check(b, plain, b.run())
-    for t in tracers:  # back to the default builder for the other tests
+    for t in tracers:  # back to the default builder and width for the other tests
         t.build_bvh()
 
 

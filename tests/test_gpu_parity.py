@@ -35,9 +35,9 @@ def _energy(h):
     return (np.asarray(h, np.float64) ** 2).sum(-1)
 
 
-def _check_debug(w, nrays, max_record, bands=(0, 1, 2), builder="default", **over):
+def _check_debug(w, nrays, max_record, bands=(0, 1, 2), builder="default", width=0, **over):
     kw = _kw(w, num_rays=nrays, **over)
-    with _tracer(w, builder=builder) as tr:
+    with _tracer(w, builder=builder, width=width) as tr:
         for band in bands:
             hit, bt, vis = tr.trace_debug(w.source, w.recorders, band=band, max_record=max_record,
                                           exact=True, **kw)
@@ -66,9 +66,11 @@ def test_hits_bit_exact_relief_hall():
 
 
 @pytest.mark.parametrize("builder", ["lbvh", "ploc"])
-def test_hits_bit_exact_every_builder(builder):
-    _check_debug(scenes.small_test_room(), 2000, 64, builder=builder)
-    _check_debug(scenes.relief_hall(), 64, 120, bands=(2,), builder=builder)
+@pytest.mark.parametrize("width", [2, 4])
+def test_hits_bit_exact_every_builder(builder, width):
+    _check_debug(scenes.small_test_room(), 2000, 64, builder=builder, width=width)
+    _check_debug(scenes.shoebox(), 1000, 50, bands=(0,), builder=builder, width=width)
+    _check_debug(scenes.relief_hall(), 64, 120, bands=(2,), builder=builder, width=width)
 
 
 def test_builders_find_the_same_hits():
@@ -81,7 +83,8 @@ def test_builders_find_the_same_hits():
     kw = dict(render, num_rays=3000, num_bins=44100)
     ref = None
     for builder, extra in [("lbvh", {}), ("ploc", {}), ("ploc", {"ploc_radius": 4}),
-                           ("lbvh", {"max_leaf": 4})]:
+                           ("lbvh", {"max_leaf": 4}), ("lbvh", {"width": 4}),
+                           ("ploc", {"width": 4}), ("lbvh", {"max_leaf": 4, "width": 4})]:
         with Tracer(r.vertices, r.material_ids, r.materials, builder=builder, **extra) as tr:
             got = tr.trace_debug(r.sources[0], r.listeners, band=0, max_record=80, exact=True, **kw)
             info = tr.info()
@@ -93,9 +96,9 @@ def test_builders_find_the_same_hits():
                 np.testing.assert_array_equal(a, b)
 
 
-def _check_render(w, nrays, builder="default", **over):
+def _check_render(w, nrays, builder="default", width=0, **over):
     kw = _kw(w, num_rays=nrays, **over)
-    with _tracer(w, builder=builder) as tr:
+    with _tracer(w, builder=builder, width=width) as tr:
         res = tr.render(w.source, w.recorders, exact=True, **kw)
     ref = oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
                         threads=THREADS, **kw)
@@ -122,6 +125,12 @@ def test_render_exact_small_room():
 
 def test_render_exact_small_room_ploc():
     _check_render(scenes.small_test_room(), 4000, builder="ploc")
+
+
+def test_render_exact_every_width():
+    for width in (2, 4):
+        _check_render(scenes.shoebox(), 5000, width=width)
+        _check_render(scenes.relief_hall(), 300, width=width, bands=(1,))
 
 
 def test_render_exact_shoebox():
