@@ -558,15 +558,20 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* 
                                             int* s_last) {
   const DevRecorder& R = a.recs[(MODE == kModeBatch ? st.rec_base : 0) + ri];
   const V3 sdir = sub(mk(R.loc[0], R.loc[1], R.loc[2]), st.o);
+  const int k = st.k;
+  const V3 lsdir = normalized(sdir);
+  const float dt = k ? dot(lsdir, vx.n) : 1.0f;
+  // The reference tests the orientation after the visibility
+  // (src/Scene.cpp:194-208); a recorder behind the surface contributes
+  // nothing either way, so its visibility test is skipped -- except for the
+  // debug record, whose mask reports every recorder's visibility.
+  if (MODE != kModeDebug && !(dt > 0)) return false;
   c.shadow++;
   const float len = length(sdir);
   Hit hh;
   const SceneRef S = scene_of<MODE>(a, s_scenes, st);
   const float slack = 2.44140625e-4f + S.box_pad / len;
   if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
-  const int k = st.k;
-  const V3 lsdir = normalized(sdir);
-  const float dt = k ? dot(lsdir, vx.n) : 1.0f;
   if (!(dt > 0)) return true;
   float I = vx.before;
   if (k) {

@@ -548,13 +548,18 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
       uint32_t vis = 0;
       for (size_t ri = 0; ri < recs.size(); ++ri) {
         const ORec& rec = recs[ri];
-        // Scene::Connect (src/Scene.cpp:84-96)
+        // Scene::Connect (src/Scene.cpp:84-96).  The reference tests the
+        // orientation dot > 0 after the visibility; a recorder behind the
+        // surface contributes nothing either way, so its visibility test is
+        // skipped (and not counted) unless the debug record needs the mask.
         const V3 sdir = sub(rec.loc, o);
+        const V3 lsdir = normalized(sdir);
+        const float dt = k ? dot(lsdir, n) : 1.0f;
+        const bool record_vis = dbg_on && k >= 1 && k <= dbg.max_record;
+        if (!(dt > 0) && !record_vis) continue;
         cnt.shadow++;
         if (segment_blocked(sc, o, sdir)) continue;
         vis |= 1u << (ri & 31);
-        const V3 lsdir = normalized(sdir);
-        const float dt = k ? dot(lsdir, n) : 1.0f;
         if (!(dt > 0)) continue;
         float I = before;
         if (k) {

@@ -50,8 +50,12 @@ def test_adjoint_matches_oracle_fp64(raw):
 
 
 def test_pathwise_gradient_matches_central_differences():
-    """Opaque materials: d/d(absorption) of sum(g * h) by the adjoint equals
-    central differences (step 1e-3, common random numbers) to 1e-3."""
+    """Opaque materials: d/d(absorption) of sum(g * h) by the GPU adjoint
+    equals central differences (step 1e-3, common random numbers) to 1e-3.
+    The differenced losses are FP64 re-accumulations of the same paths (the
+    oracle: exact kernels trace bit-identical paths), because float atomics
+    accumulate the GPU histograms in a varying order whose rounding is close
+    to the 1e-3-step difference itself."""
     w, _, _ = scenes.inverse_shoebox()
     a = np.full((8, 3), 0.2)
     r = np.zeros((8, 3))
@@ -66,9 +70,9 @@ def test_pathwise_gradient_matches_central_differences():
                                     raw_last=fwd.raw_last_sample, **kw)
 
         def loss(aa):
-            tr.set_materials(_mats(aa, r))
-            h = tr.render(w.source, w.recorders, **kw).hist
-            return float((h.astype(np.float64) * g).sum())
+            h = oracle.render(w.vertices, w.material_ids, _mats(aa, r), w.source, w.recorders,
+                              threads=THREADS, **kw)["hist64"]
+            return float((h * g.astype(np.float64)).sum())
 
         h = 1e-3
         for m, b in [(0, 0), (3, 1), (6, 2), (1, 1)]:
