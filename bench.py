@@ -23,9 +23,10 @@ roofline   algorithmic bytes of the trace kernel (64 B per node visit, 48 B
 cpu_baseline  the CPU restatement of the reference algorithm (brute-force
            triangle loops, oracle/), all host threads, on a bounded ray sample.
 
-Multi-GPU (torchrun): rays are independent, so every rank renders its own
-rays (seed + rank) with no collective in the data path ("weak" scaling);
-rank 0 prints the max-over-ranks time.
+Multi-GPU (torchrun): rays are independent, so rank r renders rays
+[r*N, (r+1)*N) of the same random stream (ear_render_params.first_ray) with
+no collective in the data path ("weak" scaling); their raw histograms sum to
+one render of world*N rays.  Rank 0 prints the max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -385,7 +386,9 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     w = load_workload(args.workload, args.rays)
     kw = dict(w.render)
-    kw["seed"] = int(kw.get("seed", 0)) + rank
+    # rank r traces rays [r*N, (r+1)*N) of the same random stream: the
+    # ranks' raw histograms sum to one render of world*N rays
+    kw["first_ray"] = rank * int(kw["num_rays"])
     exact = args.exact
     tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad,
                     builder=args.builder, width=args.width)

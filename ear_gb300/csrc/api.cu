@@ -367,7 +367,8 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   if (p->num_bins <= 0 || p->num_bins > (1 << 30)) return fail(EAR_ERR_INVALID_ARG, "bad num_bins");
   if (bands_mask == 0 || (bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
   if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
-  if (p->num_rays > (1ull << 47)) return fail(EAR_ERR_INVALID_ARG, "num_rays above 2^47");
+  if (p->num_rays > (1ull << 47) || p->first_ray > (1ull << 47) - p->num_rays)
+    return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   if (src->num_emitter_triangles < 0 || (src->num_emitter_triangles > 0 && !src->emitter_vertices))
     return fail(EAR_ERR_INVALID_ARG, "bad emitter triangles");
   std::vector<DevRecorder> dr;
@@ -398,6 +399,7 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
     a.air[b] = 1.0f - p->air_absorption[b];
   }
   a.num_rays = p->num_rays;
+  a.ray0 = p->first_ray;
   a.num_items = p->num_rays * (uint64_t)nb;
   a.max_bounces = p->max_bounces;
   a.cutoff = p->cutoff;
@@ -910,7 +912,8 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     return fail(EAR_ERR_INVALID_ARG, "ear_render_noalloc: hist must be 16-byte aligned");
   if (p->bands_mask == 0 || (p->bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
   if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
-  if (p->num_rays > (1ull << 47)) return fail(EAR_ERR_INVALID_ARG, "num_rays above 2^47");
+  if (p->num_rays > (1ull << 47) || p->first_ray > (1ull << 47) - p->num_rays)
+    return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   DevRecorder dr[kMaxRecorders];
   int tracks = 0;
   for (int i = 0; i < nrec; ++i) {
@@ -961,6 +964,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     a.air[b] = 1.0f - p->air_absorption[b];
   }
   a.num_rays = p->num_rays;
+  a.ray0 = p->first_ray;
   a.num_items = p->num_rays * (uint64_t)nb;
   a.max_bounces = p->max_bounces;
   a.cutoff = p->cutoff;

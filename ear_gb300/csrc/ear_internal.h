@@ -130,8 +130,9 @@ struct TraceArgs {
   float emitter_total_area;
   // rng
   uint32_t k0, k1, context;
-  // work: item w -> band = bands[w / num_rays], ray = w % num_rays
+  // work: item w -> band = bands[w / num_rays], ray = ray0 + w % num_rays
   uint64_t num_rays;
+  uint64_t ray0;
   uint64_t num_items;
   int bands[3];
   int max_bounces;

@@ -613,9 +613,10 @@ template <int MODE>
 __device__ __forceinline__ void debug_put(const TraceArgs& a, const PathState& st, int k, int hit,
                                           int bt, uint32_t vis, int what) {
   if (MODE != kModeDebug) return;
-  if (st.band != a.dbg_band || (int64_t)st.ray >= a.dbg_rays || k < 1 || k > a.dbg_max_record)
+  const uint64_t local = st.ray - a.ray0;
+  if (st.band != a.dbg_band || local >= (uint64_t)a.dbg_rays || k < 1 || k > a.dbg_max_record)
     return;
-  const size_t i = (size_t)st.ray * a.dbg_max_record + (k - 1);
+  const size_t i = (size_t)local * a.dbg_max_record + (k - 1);
   if (what == 0) a.dbg_hit[i] = hit;
   if (what == 1) a.dbg_bt[i] = (uint8_t)bt;
   if (what == 2) a.dbg_vis[i] = vis;
@@ -904,7 +905,7 @@ __global__ void __launch_bounds__(kTraceMaxBlock, 4) trace_kernel(const TraceArg
           } else {
             const uint64_t bi = w / a.num_rays;
             st.band = a.bands[bi < 3 ? bi : 0];
-            st.ray = w - bi * a.num_rays;
+            st.ray = a.ray0 + (w - bi * a.num_rays);
           }
           fresh = true;
         } else {

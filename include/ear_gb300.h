@@ -156,6 +156,12 @@ typedef struct ear_render_params {
   uint32_t flags;          /* EAR_FLAG_* */
   int32_t reserved0;
   void* stream;            /* cudaStream_t, NULL = default stream */
+  uint64_t first_ray;      /* index of this call's first ray: rays
+                              first_ray .. first_ray + num_rays - 1 are traced
+                              (first_ray + num_rays <= 2^47).  A render split
+                              by ray range over calls or GPUs, each with
+                              EAR_FLAG_RAW, sums to the unsplit raw render;
+                              the 1/N and gain^2 scaling is then applied once. */
 } ear_render_params;
 
 /* Selects the tree the traversal uses (2 or 4, see ear_bvh_opts.width)

@@ -415,6 +415,7 @@ struct Emitter {
 
 struct Debug {
   int band = -1;
+  uint64_t first = 0;  // the call's first ray (ear_render_params.first_ray)
   int64_t rays = 0;
   int max_record = 0;
   int32_t* hit_tri = nullptr;
@@ -431,7 +432,8 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
                const Rng& rng, uint64_t ray, int band, float air, double cutoff,
                int max_bounces, PowFn pw, Sink& sk, Counters& cnt, const Debug& dbg) {
   const bool mesh_source = em != nullptr;
-  const bool dbg_on = dbg.band == band && (int64_t)ray < dbg.rays;
+  const uint64_t local = ray - dbg.first;  // debug records are per call
+  const bool dbg_on = dbg.band == band && local < (uint64_t)dbg.rays;
   float intensity = 1.0f;
   float total_path_length = 0.0f;
   V3 prev_ray_dir = {0.0f, 0.0f, 0.0f};
@@ -489,7 +491,7 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
       cnt.segments++;
       float t;
       const int hit = closest_hit(sc, o, d, &t);
-      if (dbg_on && k <= dbg.max_record) dbg.hit_tri[ray * dbg.max_record + (k - 1)] = hit;
+      if (dbg_on && k <= dbg.max_record) dbg.hit_tri[local * dbg.max_record + (k - 1)] = hit;
       if (hit < 0) break;
       const OTri& tr = sc.tris[(size_t)hit];
       const V3 p = {o.x + d.x * t, o.y + d.y * t, o.z + d.z * t};
@@ -538,7 +540,7 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
       total_path_length += l;
       o = p;
       d = v;
-      if (dbg_on && k <= dbg.max_record) dbg.bounce_type[ray * dbg.max_record + (k - 1)] = (uint8_t)bt;
+      if (dbg_on && k <= dbg.max_record) dbg.bounce_type[local * dbg.max_record + (k - 1)] = (uint8_t)bt;
     }
     if (k > 0) intensity *= sc.mats[(size_t)mat].survival[band];
     const float before = intensity;
@@ -592,7 +594,7 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
           }
         }
       }
-      if (dbg_on && k >= 1 && k <= dbg.max_record) dbg.visible[ray * dbg.max_record + (k - 1)] = vis;
+      if (dbg_on && k >= 1 && k <= dbg.max_record) dbg.visible[local * dbg.max_record + (k - 1)] = vis;
     }
     if ((double)intensity < cutoff) break;
     prev_ray_dir = normalized(d);
@@ -729,6 +731,7 @@ int render_impl(const ear_scene_desc* desc, const ear_source* source,
   const Rng rng0 = {(uint32_t)params->seed, (uint32_t)(params->seed >> 32), params->context, 0};
   const V3 src = load3(source->location);
   Debug dbg;
+  dbg.first = params->first_ray;
   if (out->hit_tri && out->bounce_type && out->visible && out->debug_max_record > 0) {
     dbg.band = out->debug_band;
     dbg.rays = out->debug_rays;
@@ -780,7 +783,7 @@ int render_impl(const ear_scene_desc* desc, const ear_source* source,
       const uint64_t lo = N * (uint64_t)tid / (uint64_t)nthreads;
       const uint64_t hi = N * (uint64_t)(tid + 1) / (uint64_t)nthreads;
       for (uint64_t r = lo; r < hi; ++r)
-        trace_ray(sc, mesh_source ? &em : nullptr, src, recs, rng, r, band, air,
+        trace_ray(sc, mesh_source ? &em : nullptr, src, recs, rng, params->first_ray + r, band, air,
                   params->cutoff, params->max_bounces, pw, sk, cnts[(size_t)tid], dbg);
     };
     if (nthreads == 1) {

@@ -207,3 +207,21 @@ def test_fast_mode_statistics():
     t_r = post.calc_t60(ref["hist32"][:, 1:2], ref["first_sample"][:, 1:2],
                         ref["last_sample"][:, 1:2])
     assert abs(t_f - t_r) <= 0.02 * max(t_r, 1e-9) + 1.0 / 44100, (t_f, t_r)
+
+
+def test_split_by_ray_range_equals_whole_render():
+    """first_ray: two raw half renders add up to the whole raw render (the
+    same paths: identical counters; energies within float accumulation)."""
+    w = scenes.relief_hall()
+    kw = _kw(w, num_rays=3000, raw=True)
+    with _tracer(w) as tr:
+        whole = tr.render(w.source, w.recorders, exact=True, **kw)
+        parts = [tr.render(w.source, w.recorders, exact=True, **dict(kw, num_rays=1500, first_ray=f))
+                 for f in (0, 1500)]
+    for key in ("rays", "segments", "shadow_queries", "contributions"):
+        assert parts[0].stats[key] + parts[1].stats[key] == whole.stats[key], key
+    summed = parts[0].hist.astype(np.float64) + parts[1].hist
+    e1, e2 = _energy(summed), _energy(whole.hist)
+    assert (np.abs(e1 - e2) <= 1e-5 * np.maximum(e2, 1e-30)).all()
+    assert (np.minimum(parts[0].first_sample, parts[1].first_sample) == whole.first_sample).all()
+    assert (np.maximum(parts[0].last_sample, parts[1].last_sample) == whole.last_sample).all()

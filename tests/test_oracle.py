@@ -229,3 +229,21 @@ def test_oracle_adjoint_raw_and_scaled_differ_by_the_finalize_scaling():
                          threads=THREADS, **kw)
     assert np.abs(raw).max() > 0
     np.testing.assert_allclose(fin, raw / kw["num_rays"], rtol=1e-6, atol=1e-12 * np.abs(raw).max())
+
+
+def test_split_by_ray_range_sums_to_the_unsplit_render():
+    """Rays first_ray .. first_ray+N-1 of the same stream: two halves with
+    raw histograms add up to the whole (FP64 re-accumulation)."""
+    w = scenes.small_test_room()
+    kw = dict(w.render, num_rays=600, raw=True)
+    whole = oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
+                          threads=THREADS, **kw)
+    parts = [oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
+                           threads=THREADS, **dict(kw, num_rays=300, first_ray=f))
+             for f in (0, 300)]
+    np.testing.assert_allclose(parts[0]["hist64"] + parts[1]["hist64"], whole["hist64"],
+                               rtol=1e-12, atol=1e-12 * np.abs(whole["hist64"]).max())
+    for k in whole["counters"]:
+        assert parts[0]["counters"][k] + parts[1]["counters"][k] == whole["counters"][k]
+    assert (np.minimum(parts[0]["first_sample"], parts[1]["first_sample"]) == whole["first_sample"]).all()
+    assert (np.maximum(parts[0]["last_sample"], parts[1]["last_sample"]) == whole["last_sample"]).all()
