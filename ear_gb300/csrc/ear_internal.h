@@ -12,7 +12,7 @@ namespace ear {
 // BVH2 node, 64 bytes, both child boxes stored in the parent so one visit
 // tests two boxes with four 16-byte loads.  Child index >= 0 is an internal
 // node; < 0 is a leaf: ~child = first triangle (leaf order) | (count-1) << 27.
-struct __align__(16) Node {
+struct __align__(32) Node {
   float4 a;  // c0.lo.x c0.hi.x c0.lo.y c0.hi.y
   float4 b;  // c0.lo.z c0.hi.z c1.lo.x c1.hi.x
   float4 c;  // c1.lo.y c1.hi.y c1.lo.z c1.hi.z
@@ -23,7 +23,7 @@ struct __align__(16) Node {
 // even depth, each with the up to four grandchildren (or leaf children) of
 // its subtree as children.  Boxes per axis for the four slots; a child >= 0
 // is an internal Node4, < 0 a leaf code as in Node.
-struct __align__(16) Node4 {
+struct __align__(32) Node4 {
   float4 lox, hix, loy, hiy, loz, hiz;
   int4 child;
   int4 meta;  // x: parent Node4 (-1 at the root), y: mask of occupied slots
