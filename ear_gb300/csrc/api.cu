@@ -318,7 +318,7 @@ ear_status ear_scene_info(const ear_scene* s, int64_t* num_triangles, int64_t* n
   if (box_pad) *box_pad = s->ds.box_pad;
   if (device_bytes)
     *device_bytes = (int64_t)(s->ds.num_nodes * sizeof(Node) + s->ds.num_nodes4 * sizeof(Node4) +
-                              s->ds.num_tris * (48 + 16 + 36 + 4));
+                              s->ds.num_tris * (64 + 36 + 4));
   return EAR_OK;
 }
 
@@ -328,7 +328,6 @@ void ear_scene_destroy(ear_scene* s) {
   cudaFree(s->ds.nodes);
   cudaFree(s->ds.nodes4);
   cudaFree(s->ds.tris);
-  cudaFree(s->ds.nrm);
   cudaFree(s->ds.vertices);
   cudaFree(s->ds.mat_ids);
   cudaFree(s->mats);
@@ -382,7 +381,6 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   a.nodes4 = s->ds.nodes4;
   a.wide = s->ds.wide;
   a.tris = s->ds.tris;
-  a.nrm = s->ds.nrm;
   a.num_tris = (int)s->ds.num_tris;
   a.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   a.mats = s->mats;
@@ -945,7 +943,6 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.nodes4 = s->ds.nodes4;
   a.wide = s->ds.wide;
   a.tris = s->ds.tris;
-  a.nrm = s->ds.nrm;
   a.num_tris = (int)s->ds.num_tris;
   a.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   a.mats = s->mats;

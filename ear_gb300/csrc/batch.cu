@@ -90,7 +90,7 @@ SceneRef scene_ref(const ear_scene* s, int mat_base) {
   r.wide = s->ds.wide;
   r.pad = 0;
   r.tris = s->ds.tris;
-  r.nrm = s->ds.nrm;
+  r.shade = s->ds.tris ? s->ds.tris + 3 : nullptr;
   r.num_tris = (int)s->ds.num_tris;
   r.num_nodes = (int)(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes);
   r.box_pad = s->ds.box_pad;

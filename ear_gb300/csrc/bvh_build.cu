@@ -442,8 +442,7 @@ __global__ void k_depth(const int32_t* __restrict__ leaf_parent, int n, const No
 
 // Gather triangles into leaf order with edges, normals and materials.
 __global__ void k_gather(const float* __restrict__ v, const int32_t* __restrict__ mat_ids,
-                         const int32_t* __restrict__ sorted_idx, int n, float4* __restrict__ tris,
-                         float4* __restrict__ nrm) {
+                         const int32_t* __restrict__ sorted_idx, int n, float4* __restrict__ tris) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const int t = sorted_idx[j];
@@ -451,10 +450,10 @@ __global__ void k_gather(const float* __restrict__ v, const int32_t* __restrict_
   const V3 a = mk(p[0], p[1], p[2]), b = mk(p[3], p[4], p[5]), c = mk(p[6], p[7], p[8]);
   const V3 e1 = sub(b, a), e2 = sub(c, a);
   const V3 nn = normalized(cross(e1, e2));
-  tris[3 * j + 0] = make_float4(a.x, a.y, a.z, __int_as_float(t));
-  tris[3 * j + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
-  tris[3 * j + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
-  nrm[j] = make_float4(nn.x, nn.y, nn.z, __int_as_float(mat_ids[t]));
+  tris[4 * j + 0] = make_float4(a.x, a.y, a.z, __int_as_float(t));
+  tris[4 * j + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+  tris[4 * j + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+  tris[4 * j + 3] = make_float4(nn.x, nn.y, nn.z, __int_as_float(mat_ids[t]));
 }
 
 // Single-triangle scene: a root whose two children are the same leaf.
@@ -522,10 +521,8 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   s.num_nodes4 = 0;
   s.depth4 = 0;
   if (s.tris) cudaFree(s.tris);
-  if (s.nrm) cudaFree(s.nrm);
   s.nodes = nullptr;
   s.tris = nullptr;
-  s.nrm = nullptr;
   s.num_nodes = 0;
   if (n == 0) {
     s.max_depth = 0;
@@ -546,8 +543,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   CK(cudaMalloc(&range, sizeof(int2) * nn));
   CK(cudaMalloc(&dmax, sizeof(int)));
   CK(cudaMalloc(&s.nodes, sizeof(Node) * nn));
-  CK(cudaMalloc(&s.tris, sizeof(float4) * 3 * (size_t)n));
-  CK(cudaMalloc(&s.nrm, sizeof(float4) * (size_t)n));
+  CK(cudaMalloc(&s.tris, sizeof(float4) * 4 * (size_t)n));
   {
     const uint32_t init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0u};
     CK(cudaMemcpyAsync(bounds, init, sizeof init, cudaMemcpyHostToDevice, stream));
@@ -690,7 +686,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
       goto done;
     }
   }
-  k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris, s.nrm);
+  k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(stream));
   s.num_nodes = nn;

@@ -33,10 +33,10 @@ constexpr int kMaxDepth4 = 32;  // levels of the 128-bit traversal trail
 constexpr int kLeafCountShift = 27;
 constexpr int kLeafStartMask = (1 << kLeafCountShift) - 1;
 
-// Triangles in leaf order, 48 bytes each for the Moller-Trumbore test:
-//   tri[3i+0] = (v0.xyz, original index as int bits)
-//   tri[3i+1] = (e1 = v1 - v0, 0), tri[3i+2] = (e2 = v2 - v0, 0)
-// and 16 bytes of shading data: nrm[i] = (unit normal, material id bits).
+// Triangles in leaf order, 64 bytes each (two 32-byte loads):
+//   tri[4i+0] = (v0.xyz, original index as int bits)
+//   tri[4i+1] = (e1 = v1 - v0, 0), tri[4i+2] = (e2 = v2 - v0, 0)
+//   tri[4i+3] = (unit normal, material id bits), read once per hit.
 
 struct DeviceScene {
   int64_t num_tris = 0;
@@ -51,7 +51,6 @@ struct DeviceScene {
   int64_t num_nodes4 = 0;
   int depth4 = 0;
   float4* tris = nullptr;
-  float4* nrm = nullptr;
   // inputs kept on the device in file order
   float* vertices = nullptr;  // [n][9]
   int32_t* mat_ids = nullptr;
@@ -85,7 +84,7 @@ struct __align__(16) SceneRef {
   const Node* nodes2;   // binary tree
   const Node4* nodes4;  // 4-wide tree
   const float4* tris;
-  const float4* nrm;
+  const float4* shade;  // tris + 3: shading data at stride 4
   int num_tris;
   int num_nodes;  // nodes of the tree in use
   float box_pad;
@@ -116,7 +115,6 @@ struct TraceArgs {
   const Node4* nodes4;
   int wide;
   const float4* tris;
-  const float4* nrm;
   int num_tris;
   int num_nodes;
   const DevMaterial* mats;

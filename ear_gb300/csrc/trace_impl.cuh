@@ -151,8 +151,10 @@ __device__ __forceinline__ bool leaf_test(const SceneRef& S, int code, V3 o, V3 
   c.tris += (uint32_t)cnt;
   bool blocked = false;
   for (int k = 0; k < cnt; ++k) {
-    const float4* T = S.tris + 3 * (start + k);
-    const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
+    const float4* T = S.tris + 4 * (start + k);
+    float4 A, B, C, Nn;
+    ldg256(T, A, B);
+    ldg256(T + 2, C, Nn);
     float t;
     if (mt_intersect(A, B, C, o, d, t)) {
       if (ANY) {
@@ -540,7 +542,7 @@ __device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef*
   S.nodes4 = a.nodes4;
   S.wide = a.wide;
   S.tris = a.tris;
-  S.nrm = a.nrm;
+  S.shade = a.tris + 3;
   S.num_tris = a.num_tris;
   S.num_nodes = a.num_nodes;
   S.box_pad = a.box_pad;
@@ -710,7 +712,7 @@ __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict_
   traverse<false>(S, st.o, st.d, 1000000.0f, S.box_pad, h, c, err);
   debug_put<MODE>(a, st, k, h.pos >= 0 ? h.orig : -1, 0, 0, 0);
   if (h.pos < 0) return false;
-  const float4 nm = __ldg(S.nrm + h.pos);
+  const float4 nm = __ldg(S.shade + 4 * h.pos);
   const float t = h.t;
   const V3 p = mk(st.o.x + st.d.x * t, st.o.y + st.d.y * t, st.o.z + st.d.z * t);
   const V3 N = mk(nm.x, nm.y, nm.z);
