@@ -651,8 +651,12 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
   CU(cudaMemcpy(b->d_trial_jobs, tj.data(), sizeof(BatchJob) * tj.size(), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(b->d_trial_end, tend.data(), sizeof(uint64_t) * tend.size(), cudaMemcpyHostToDevice));
 
+  // leaf sizes apply to LBVH scenes only (PLOC builds single-triangle leaves)
+  bool all_lbvh = true;
+  for (const ear_scene* sc : b->scenes) all_lbvh = all_lbvh && sc->ds.builder != kBuilderPloc;
+  const bool tune_leaf = o.tune_leaf_size && all_lbvh;
   std::vector<int> leaves = {b->cfg.max_leaf_size > 0 ? b->cfg.max_leaf_size : 1};
-  if (o.tune_leaf_size) leaves = {1, 2, 4};
+  if (tune_leaf) leaves = {1, 2, 4};
   const int blocks[] = {128, 256};
   std::vector<int> widths = {0};
   if (o.tune_width) widths = {2, 4};
@@ -661,7 +665,7 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
   bool have = false;
   for (int leaf : leaves)
   for (int width : widths) {
-    if (o.tune_leaf_size) {
+    if (tune_leaf) {
       const ear_status rc = rebuild_scenes(b, leaf);
       if (rc != EAR_OK) return rc;
       b->cfg.max_leaf_size = leaf;
@@ -707,7 +711,7 @@ ear_status ear_batch_tune(ear_batch* b, const ear_tune_opts* opts, ear_tune_resu
       }
     }
   }
-  if (o.tune_leaf_size) {
+  if (tune_leaf) {
     const ear_status rc = rebuild_scenes(b, best.max_leaf_size);
     if (rc != EAR_OK) return rc;
     b->cfg.max_leaf_size = best.max_leaf_size;
