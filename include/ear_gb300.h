@@ -108,7 +108,7 @@ typedef struct ear_bvh_opts {
      cost, single-triangle leaves).  Never changes which triangle is
      reported. */
   int32_t builder;
-  int32_t ploc_radius;     /* PLOC search radius in positions (0 = 16) */
+  int32_t ploc_radius;     /* PLOC search radius in positions (0 = 4) */
   /* Tree the traversal uses: 2 (binary), 4 (4-wide, built from the binary
      tree: fewer dependent node loads per query, costlier visits) or 0 =
      4-wide from 4096 triangles on.  Both trees are built; the choice can
