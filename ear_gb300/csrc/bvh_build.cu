@@ -364,70 +364,108 @@ __global__ void k_permute(const Node* __restrict__ nodes, const int* __restrict_
 }
 
 // ------------------------------------------------------------- 4-wide
-// The binary nodes at even depth become 4-wide nodes whose children are the
-// binary grandchildren (or leaf children) of their subtree, in binary
-// order; their indices follow the binary order through a prefix sum, so
-// the depth-first layout carries over and the root stays node 0.
-__global__ void k_node_depth(const Node* __restrict__ nodes, int nn, int* __restrict__ depth,
-                             int* __restrict__ even) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nn) return;
-  int d = 0;
-  for (int cur = v; d < 4096; ++d) {
-    const int par = nodes[cur].d.z;
-    if (par < 0) break;
-    cur = par;
-  }
-  depth[v] = d;
-  even[v] = (d & 1) ? 0 : 1;
+// 4-wide nodes, built top-down from the binary tree one frontier (level) at
+// a time.  A 4-wide node starts from its binary node's two children and
+// repeatedly opens the internal child with the largest surface area until
+// it has four children (or only leaves are left) -- the usual greedy
+// collapse, which fills the slots that grouping fixed pairs of levels
+// leaves empty near the leaves.  The internal children of a level's nodes
+// are numbered consecutively through a prefix sum (deterministic), so a
+// node's internal children are neighbours in memory; the root is node 0.
+struct Slot4 {
+  float lo[3], hi[3];
+  int ref;  // >= 0 binary internal node, < 0 leaf code
+};
+
+__device__ __forceinline__ Slot4 slot_of(const Node& P, int c) {
+  Slot4 s;
+  s.lo[0] = c ? P.b.z : P.a.x;
+  s.hi[0] = c ? P.b.w : P.a.y;
+  s.lo[1] = c ? P.c.x : P.a.z;
+  s.hi[1] = c ? P.c.y : P.a.w;
+  s.lo[2] = c ? P.c.z : P.b.x;
+  s.hi[2] = c ? P.c.w : P.b.y;
+  s.ref = c ? P.d.y : P.d.x;
+  return s;
 }
 
-__global__ void k_build4(const Node* __restrict__ nodes, int nn, const int* __restrict__ depth,
-                         const int* __restrict__ idx4, Node4* __restrict__ out,
-                         int* __restrict__ max_depth4) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nn || (depth[v] & 1)) return;
-  const Node P = nodes[v];
-  float lx[4] = {0, 0, 0, 0}, hx[4] = {0, 0, 0, 0}, ly[4] = {0, 0, 0, 0}, hy[4] = {0, 0, 0, 0};
-  float lz[4] = {0, 0, 0, 0}, hz[4] = {0, 0, 0, 0};
-  int ch[4] = {0, 0, 0, 0};
-  int k = 0;
-  for (int c = 0; c < 2; ++c) {
-    const int cc = c == 0 ? P.d.x : P.d.y;
-    if (c == 1 && cc == P.d.x && cc < 0) break;  // the single-triangle root
-    // box of binary child c, as stored in P
-    const float bx0 = c ? P.b.z : P.a.x, bx1 = c ? P.b.w : P.a.y;
-    const float by0 = c ? P.c.x : P.a.z, by1 = c ? P.c.y : P.a.w;
-    const float bz0 = c ? P.c.z : P.b.x, bz1 = c ? P.c.w : P.b.y;
-    if (cc < 0) {
-      lx[k] = bx0; hx[k] = bx1; ly[k] = by0; hy[k] = by1; lz[k] = bz0; hz[k] = bz1;
-      ch[k] = cc;
-      ++k;
-      continue;
+__device__ __forceinline__ float slot_area(const Slot4& s) {
+  const float dx = s.hi[0] - s.lo[0], dy = s.hi[1] - s.lo[1], dz = s.hi[2] - s.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// Expands the frontier's binary nodes into up to four slots each and
+// counts their internal slots.
+__global__ void k_expand4(const Node* __restrict__ nodes, const int* __restrict__ frontier, int nf,
+                          Slot4* __restrict__ slots, int* __restrict__ nslots,
+                          int* __restrict__ ninternal) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const Node P = nodes[frontier[f]];
+  Slot4 s[4];
+  int n = 0;
+  s[n++] = slot_of(P, 0);
+  if (!(P.d.y == P.d.x && P.d.x < 0)) s[n++] = slot_of(P, 1);  // the single-triangle root
+  while (n < 4) {
+    int best = -1;
+    float area = -1.0f;
+    for (int j = 0; j < n; ++j)
+      if (s[j].ref >= 0 && slot_area(s[j]) > area) {
+        area = slot_area(s[j]);
+        best = j;
+      }
+    if (best < 0) break;
+    const Node C = nodes[s[best].ref];
+    s[n++] = slot_of(C, 1);
+    s[best] = slot_of(C, 0);
+  }
+  int internal = 0;
+  for (int j = 0; j < 4; ++j) {
+    if (j < n) {
+      slots[4 * f + j] = s[j];
+      internal += s[j].ref >= 0 ? 1 : 0;
     }
-    const Node C = nodes[cc];
-    for (int g = 0; g < 2; ++g) {
-      const int gg = g == 0 ? C.d.x : C.d.y;
-      lx[k] = g ? C.b.z : C.a.x; hx[k] = g ? C.b.w : C.a.y;
-      ly[k] = g ? C.c.x : C.a.z; hy[k] = g ? C.c.y : C.a.w;
-      lz[k] = g ? C.c.z : C.b.x; hz[k] = g ? C.c.w : C.b.y;
-      ch[k] = gg < 0 ? gg : idx4[gg];
-      ++k;
+  }
+  nslots[f] = n;
+  ninternal[f] = internal;
+}
+
+__global__ void k_write4(const Slot4* __restrict__ slots, const int* __restrict__ nslots,
+                         const int* __restrict__ ninternal, const int* __restrict__ offset, int nf,
+                         int level_base, int next_base, const int* __restrict__ parent4,
+                         Node4* __restrict__ out, int* __restrict__ next_frontier,
+                         int* __restrict__ next_parent4) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int n = nslots[f];
+  float v[6][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+  int ch[4] = {0, 0, 0, 0};
+  int r = 0;
+  for (int j = 0; j < n; ++j) {
+    const Slot4 s = slots[4 * f + j];
+    for (int a = 0; a < 3; ++a) {
+      v[2 * a][j] = s.lo[a];
+      v[2 * a + 1][j] = s.hi[a];
+    }
+    if (s.ref < 0) {
+      ch[j] = s.ref;
+    } else {
+      const int pos = offset[f] + r++;
+      ch[j] = next_base + pos;
+      next_frontier[pos] = s.ref;
+      next_parent4[pos] = level_base + f;
     }
   }
   Node4 n4;
-  n4.lox = make_float4(lx[0], lx[1], lx[2], lx[3]);
-  n4.hix = make_float4(hx[0], hx[1], hx[2], hx[3]);
-  n4.loy = make_float4(ly[0], ly[1], ly[2], ly[3]);
-  n4.hiy = make_float4(hy[0], hy[1], hy[2], hy[3]);
-  n4.loz = make_float4(lz[0], lz[1], lz[2], lz[3]);
-  n4.hiz = make_float4(hz[0], hz[1], hz[2], hz[3]);
+  n4.lox = make_float4(v[0][0], v[0][1], v[0][2], v[0][3]);
+  n4.hix = make_float4(v[1][0], v[1][1], v[1][2], v[1][3]);
+  n4.loy = make_float4(v[2][0], v[2][1], v[2][2], v[2][3]);
+  n4.hiy = make_float4(v[3][0], v[3][1], v[3][2], v[3][3]);
+  n4.loz = make_float4(v[4][0], v[4][1], v[4][2], v[4][3]);
+  n4.hiz = make_float4(v[5][0], v[5][1], v[5][2], v[5][3]);
   n4.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
-  int parent4 = -1;
-  if (P.d.z >= 0) parent4 = idx4[nodes[P.d.z].d.z];  // the binary grandparent
-  n4.meta = make_int4(parent4, (1 << k) - 1, 0, 0);
-  out[idx4[v]] = n4;
-  atomicMax(max_depth4, depth[v] / 2 + 1);
+  n4.meta = make_int4(parent4[f], (1 << n) - 1, 0, 0);
+  out[level_base + f] = n4;
 }
 
 // Depth of every leaf (internal nodes on its root path + 1).
@@ -497,9 +535,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
   int* dmax = nullptr;
   int *ssize = nullptr, *spos = nullptr;
   Node* reordered = nullptr;
-  int *ndepth = nullptr, *even = nullptr, *idx4 = nullptr, *dmax4 = nullptr;
-  void* stmp4 = nullptr;
-  size_t stmp4_bytes = 0;
+
   // PLOC
   float4 *clo = nullptr, *chi = nullptr, *clo2 = nullptr, *chi2 = nullptr;
   int *cid = nullptr, *cid2 = nullptr, *nnb = nullptr, *mflag = nullptr, *mrank = nullptr;
@@ -655,36 +691,65 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
     }
   }
   {
-    // the 4-wide tree
-    const int gn = (nn + B - 1) / B;
-    int last_even = 0, last_idx = 0, depth4 = 0;
-    CK(cudaMalloc(&ndepth, sizeof(int) * nn));
-    CK(cudaMalloc(&even, sizeof(int) * nn));
-    CK(cudaMalloc(&idx4, sizeof(int) * nn));
-    CK(cudaMalloc(&dmax4, sizeof(int)));
-    CK(cudaMemsetAsync(dmax4, 0, sizeof(int), stream));
-    k_node_depth<<<gn, B, 0, stream>>>(s.nodes, nn, ndepth, even);
-    CK(cudaGetLastError());
-    CK(cub::DeviceScan::ExclusiveSum(nullptr, stmp4_bytes, even, idx4, nn, stream));
-    CK(cudaMalloc(&stmp4, stmp4_bytes));
-    CK(cub::DeviceScan::ExclusiveSum(stmp4, stmp4_bytes, even, idx4, nn, stream));
-    CK(cudaMemcpyAsync(&last_even, even + nn - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(&last_idx, idx4 + nn - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    const int n4 = last_idx + last_even;
-    CK(cudaMalloc(&s.nodes4, sizeof(Node4) * (size_t)n4));
-    k_build4<<<gn, B, 0, stream>>>(s.nodes, nn, ndepth, idx4, s.nodes4, dmax4);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(&depth4, dmax4, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    s.num_nodes4 = n4;
-    s.depth4 = depth4;
-    if (depth4 > kMaxDepth4) {
-      snprintf(err, errlen, "4-wide BVH depth %d exceeds the %d levels of the traversal trail",
-               depth4, kMaxDepth4);
-      rc = cudaErrorInvalidValue;
-      goto done;
+    // the 4-wide tree, one level per pass
+    int *front = nullptr, *front2 = nullptr, *par4 = nullptr, *par4b = nullptr;
+    int *nsl = nullptr, *nint = nullptr, *off = nullptr;
+    Slot4* slots = nullptr;
+    void* st4 = nullptr;
+    size_t st4_bytes = 0;
+    int levels = 0, nf = 1, base = 0, total = 0;
+    const int root_parent = -1, root = 0;
+    const int cap = nn > 0 ? nn : 1;  // at most one 4-wide node per binary node
+    CK(cudaMalloc(&s.nodes4, sizeof(Node4) * (size_t)cap));
+    CK(cudaMalloc(&front, sizeof(int) * cap));
+    CK(cudaMalloc(&front2, sizeof(int) * cap));
+    CK(cudaMalloc(&par4, sizeof(int) * cap));
+    CK(cudaMalloc(&par4b, sizeof(int) * cap));
+    CK(cudaMalloc(&nsl, sizeof(int) * cap));
+    CK(cudaMalloc(&nint, sizeof(int) * cap));
+    CK(cudaMalloc(&off, sizeof(int) * cap));
+    CK(cudaMalloc(&slots, sizeof(Slot4) * 4 * (size_t)cap));
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, st4_bytes, nint, off, cap, stream));
+    CK(cudaMalloc(&st4, st4_bytes));
+    CK(cudaMemcpyAsync(front, &root, sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(par4, &root_parent, sizeof(int), cudaMemcpyHostToDevice, stream));
+    while (nf > 0) {
+      if (++levels > kMaxDepth4 || base + nf > cap) {
+        snprintf(err, errlen, "4-wide BVH deeper than the %d levels of the traversal trail",
+                 kMaxDepth4);
+        rc = cudaErrorInvalidValue;
+        break;
+      }
+      const int gf = (nf + B - 1) / B;
+      k_expand4<<<gf, B, 0, stream>>>(s.nodes, front, nf, slots, nsl, nint);
+      CK(cudaGetLastError());
+      size_t tb = st4_bytes;
+      CK(cub::DeviceScan::ExclusiveSum(st4, tb, nint, off, nf, stream));
+      int last_off = 0, last_int = 0;
+      CK(cudaMemcpyAsync(&last_off, off + nf - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&last_int, nint + nf - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      k_write4<<<gf, B, 0, stream>>>(slots, nsl, nint, off, nf, base, base + nf, par4, s.nodes4,
+                                     front2, par4b);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(stream));
+      base += nf;
+      nf = last_off + last_int;
+      std::swap(front, front2);
+      std::swap(par4, par4b);
     }
+    total = base;
+    cudaFree(front);
+    cudaFree(front2);
+    cudaFree(par4);
+    cudaFree(par4b);
+    cudaFree(nsl);
+    cudaFree(nint);
+    cudaFree(off);
+    cudaFree(slots);
+    cudaFree(st4);
+    if (rc != cudaSuccess) goto done;
+    s.num_nodes4 = total;
+    s.depth4 = levels;
   }
   k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris);
   CK(cudaGetLastError());
@@ -714,11 +779,7 @@ done:
   cudaFree(ssize);
   cudaFree(spos);
   cudaFree(reordered);
-  cudaFree(ndepth);
-  cudaFree(even);
-  cudaFree(idx4);
-  cudaFree(dmax4);
-  cudaFree(stmp4);
+
   cudaFree(clo);
   cudaFree(chi);
   cudaFree(clo2);

@@ -566,7 +566,6 @@ struct Vertex {
   V3 n;          // oriented (and, for REFRACT, flipped) surface normal
   int bt;        // 0 REFLECT, 1 REFRACT (src/Material.h:27)
   float spec;    // specularity of the hit material in this band
-  float before;  // sample_intensity_before_bounce (src/Scene.cpp:173)
   bool conn;     // connect the recorders at this vertex
 };
 
@@ -594,7 +593,9 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* 
   const float slack = 2.44140625e-4f + S.box_pad / len;
   if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
   if (!(dt > 0)) return true;
-  float I = vx.before;
+  // sample_intensity_before_bounce (src/Scene.cpp:173): the path's
+  // intensity, unchanged between the vertex and its connections
+  float I = st.I;
   if (k) {
     const V3 n = vx.n;
     float factor;
@@ -693,7 +694,6 @@ __device__ void emit_vertex(const TraceArgs& a, PathState& st, LaneCounters& c, 
   vx.n = mk(0, 0, 0);
   vx.bt = 0;
   vx.spec = 0.0f;
-  vx.before = st.I;
   vx.conn = MODE != kModeBatch && a.num_emitter > 0;
 }
 
@@ -771,7 +771,6 @@ __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict_
   vx.n = n;
   vx.bt = bt;
   vx.spec = spec;
-  vx.before = st.I;
   vx.conn = true;
   return !invalid_float(st.I);
 }
