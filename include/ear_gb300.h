@@ -94,7 +94,7 @@ typedef struct ear_scene_desc {
 
 typedef struct ear_bvh_opts {
   /* Padding added to every triangle's bounding box, in scene units.  Values
-     < 0 select the default (2^-12 of the largest absolute coordinate plus
+     < 0 select the default (2^-18 of the largest absolute coordinate plus
      1e-5).  Padding only makes the culling conservative; it never changes
      which triangle is reported. */
   float box_pad;
