@@ -37,6 +37,12 @@ namespace EAR_NS {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Relative widening of the t-range culling (2^-16, about 128 ulp of t):
+// the slab distances and the triangle test round independently, so a box
+// whose entry distance rounds just above the current best hit must not be
+// culled.  The boxes' own padding covers the rounding in space.
+constexpr float kSlackRel = 1.52587890625e-5f;
+
 // A ray for the slab tests: 1/d and -o/d, so each plane distance
 // t = (plane - o) / d is one fused multiply-add, plane * (1/d) + (-o/d).
 // Its rounding differs from (plane - o) * (1/d) by a few ulp of the
@@ -212,7 +218,7 @@ __device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     ldg256(&nd->a, na, nb);
     ldg256(&nd->c, nc, nd4);
     const int4 ch = as_int4(nd4);
-    const float lim = ANY ? tlimit + slack : h.t + (h.t * 2.44140625e-4f + slack);
+    const float lim = ANY ? tlimit + slack : h.t + (h.t * kSlackRel + slack);
     float t0, t1;
     bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
     bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
@@ -315,7 +321,7 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     ldg256(&nd->child, chf, mtf);
     const int4 ch = as_int4(chf), meta = as_int4(mtf);
     const unsigned cand = (reentry ? (unsigned)(tlo & 0xFull) : 0xFu) & (unsigned)meta.y;
-    const float lim = ANY ? tlimit + slack : h.t + (h.t * 2.44140625e-4f + slack);
+    const float lim = ANY ? tlimit + slack : h.t + (h.t * kSlackRel + slack);
     unsigned hit = 0u, leaf = 0u;
     float tk[4];
 #pragma unroll
@@ -590,7 +596,7 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* 
   const float len = length(sdir);
   Hit hh;
   const SceneRef S = scene_of<MODE>(a, s_scenes, st);
-  const float slack = 2.44140625e-4f + S.box_pad / len;
+  const float slack = kSlackRel + S.box_pad / len;
   if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
   if (!(dt > 0)) return true;
   // sample_intensity_before_bounce (src/Scene.cpp:173): the path's
@@ -818,7 +824,7 @@ __device__ void direct_visibility(const TraceArgs& a, const SceneRef* s_scenes, 
     const V3 loc = mk(R.loc[0], R.loc[1], R.loc[2]);
     const V3 seg = sub(mk(src[0], src[1], src[2]), loc);
     const float seglen = length(seg);
-    const float slack = 2.44140625e-4f + (seglen > 0.0f ? S.box_pad / seglen : 0.0f);
+    const float slack = kSlackRel + (seglen > 0.0f ? S.box_pad / seglen : 0.0f);
     LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
     Hit hh;
     const bool blocked = traverse<true>(S, loc, seg, 1.0f, slack, hh, c, err);
