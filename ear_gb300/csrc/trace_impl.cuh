@@ -97,6 +97,21 @@ __device__ __forceinline__ bool mt_intersect(const float4& A, const float4& B, c
   const V3 pvec = cross(d, e2);
   const float det = dot(e1, pvec);
   if (det > -1e-6f && det < 1e-6f) return false;
+#if EAR_FAST_TRIANGLE_TEST
+  // fast kernels: the barycentric bounds are compared unscaled, u*det and
+  // v*det against det, so only accepted candidates pay the division
+  const V3 tvec = sub(o, mk(A.x, A.y, A.z));
+  const float un = dot(tvec, pvec);
+  const V3 qvec = cross(tvec, e1);
+  const float vn = dot(d, qvec);
+  if (det > 0.0f) {
+    if (un < 0.0f || un > det || vn < 0.0f || un + vn > det) return false;
+  } else {
+    if (un > 0.0f || un < det || vn > 0.0f || un + vn < det) return false;
+  }
+  t = dot(e2, qvec) / det;
+  return true;
+#else
   const float inv_det = 1.0f / det;
   const V3 tvec = sub(o, mk(A.x, A.y, A.z));
   const float u = dot(tvec, pvec) * inv_det;
@@ -106,6 +121,7 @@ __device__ __forceinline__ bool mt_intersect(const float4& A, const float4& B, c
   if (v < 0.0f || u + v > 1.0f) return false;
   t = dot(e2, qvec) * inv_det;
   return true;
+#endif
 }
 
 // 32-byte read-only load (sm_100+ `ld.global.nc.v8`): a 4-wide node is 4
