@@ -48,7 +48,8 @@ class EarSceneDesc(C.Structure):
 
 class EarBvhOpts(C.Structure):
     _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("builder", C.c_int32),
-                ("ploc_radius", C.c_int32), ("width", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("ploc_radius", C.c_int32), ("width", C.c_int32), ("visibility_order", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class EarRecorder(C.Structure):

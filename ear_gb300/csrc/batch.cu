@@ -88,7 +88,7 @@ SceneRef scene_ref(const ear_scene* s, int mat_base) {
   r.nodes2 = s->ds.nodes;
   r.nodes4 = s->ds.nodes4;
   r.wide = s->ds.wide;
-  r.pad = 0;
+  r.any_far = s->ds.any_far;
   r.tris = s->ds.tris;
   r.shade = s->ds.tris ? s->ds.tris + 3 : nullptr;
   r.num_tris = (int)s->ds.num_tris;

@@ -46,6 +46,10 @@ struct DeviceScene {
   int max_leaf = 1;
   int builder = 1;
   int wide = 0;  // traverse the 4-wide tree
+  // order of the visibility (any-hit) tests: 0 automatic, 1 nearest hit
+  // child first, 2 farthest first; any_far is the order in use
+  int any_order = 0;
+  int any_far = 0;
   Node* nodes = nullptr;
   Node4* nodes4 = nullptr;
   int64_t num_nodes4 = 0;
@@ -91,8 +95,8 @@ struct __align__(16) SceneRef {
   int mat_base;  // first material of the scene in the launch's table
   int num_mats;
   int traverse_budget;
-  int wide;  // 1: traverse nodes4, 0: nodes2
-  int pad;
+  int wide;     // 1: traverse nodes4, 0: nodes2
+  int any_far;  // visibility tests visit the farthest hit child first
 };
 
 // One (scene, source position, recorder set) of a batch.  Its work items
@@ -114,6 +118,7 @@ struct TraceArgs {
   const Node* nodes;
   const Node4* nodes4;
   int wide;
+  int any_far;
   const float4* tris;
   int num_tris;
   int num_nodes;
@@ -198,6 +203,8 @@ struct TraceOps {
   cudaError_t (*trace)(const TraceArgs& a, int grid, int block, size_t smem, int mode,
                        cudaStream_t s);
   cudaError_t (*occupancy)(int mode, int block, size_t smem, int* blocks_per_sm);
+  // blocked count of n seeded centroid -> recorder segments (occlusion probe)
+  cudaError_t (*probe)(const TraceArgs& a, int n, unsigned* blocked, cudaStream_t s);
   int block;  // default block size
 };
 // Dynamic shared memory of a trace launch.

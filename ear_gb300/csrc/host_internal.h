@@ -116,4 +116,8 @@ struct ear_scene {
   float4* emitter = nullptr;
   size_t emitter_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // automatic visibility order: occlusion probe result for one recorder set
+  unsigned* probe = nullptr;
+  uint64_t probe_key = 0;
+  bool probe_valid = false;
 };

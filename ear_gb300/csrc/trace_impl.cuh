@@ -252,7 +252,7 @@ __device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     if (h0 || h1) {
       if (h0 && h1) {
         trail = (trail << 1) | 1ull;
-        cur = (t0 <= t1) ? ch.x : ch.y;
+        cur = ((t0 <= t1) != (ANY && S.any_far)) ? ch.x : ch.y;
       } else {
         trail <<= 1;
         cur = h0 ? ch.x : ch.y;
@@ -360,8 +360,12 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
       int kb = -1;
       float best = 0.0f;
 #pragma unroll
+      // nearest hit child first; visibility tests in scenes where most
+      // segments are blocked go farthest first (occluders between the
+      // surface and the listener are met sooner)
+      const bool far = ANY && S.any_far;
       for (int k = 0; k < 4; ++k)
-        if (((hit >> k) & 1u) && (kb < 0 || tk[k] < best)) {
+        if (((hit >> k) & 1u) && (kb < 0 || (far ? tk[k] > best : tk[k] < best))) {
           best = tk[k];
           kb = k;
         }
@@ -563,6 +567,7 @@ __device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef*
   S.nodes2 = a.nodes;
   S.nodes4 = a.nodes4;
   S.wide = a.wide;
+  S.any_far = a.any_far;
   S.tris = a.tris;
   S.shade = a.tris + 3;
   S.num_tris = a.num_tris;
@@ -592,9 +597,10 @@ struct Vertex {
 };
 
 // Visibility + contribution of recorder `ri` at the current vertex
-// (src/Scene.cpp:188-268).  Returns whether the recorder is visible.
+// (src/Scene.cpp:188-268).  Returns kNotTested, kBlockedSeg or kVisible.
+enum { kNotTested = 0, kBlockedSeg = 1, kVisible = 2 };
 template <int MODE>
-__device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* s_scenes,
+__device__ __forceinline__ int connect_one(const TraceArgs& a, const SceneRef* s_scenes,
                                             PathState& st, const Vertex& vx, int ri,
                                             LaneCounters& c, int& err, int* s_first,
                                             int* s_last) {
@@ -607,14 +613,14 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* 
   // (src/Scene.cpp:194-208); a recorder behind the surface contributes
   // nothing either way, so its visibility test is skipped -- except for the
   // debug record, whose mask reports every recorder's visibility.
-  if (MODE != kModeDebug && !(dt > 0)) return false;
+  if (MODE != kModeDebug && !(dt > 0)) return kNotTested;
   c.shadow++;
   const float len = length(sdir);
   Hit hh;
   const SceneRef S = scene_of<MODE>(a, s_scenes, st);
   const float slack = kSlackRel + S.box_pad / len;
-  if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return false;
-  if (!(dt > 0)) return true;
+  if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return kBlockedSeg;
+  if (!(dt > 0)) return kVisible;
   // sample_intensity_before_bounce (src/Scene.cpp:173): the path's
   // intensity, unchanged between the vertex and its connections
   float I = st.I;
@@ -650,7 +656,7 @@ __device__ __forceinline__ bool connect_one(const TraceArgs& a, const SceneRef* 
       st.T += G;
     }
   }
-  return true;
+  return kVisible;
 }
 
 template <int MODE>
@@ -975,9 +981,10 @@ __global__ void __launch_bounds__(kTraceMaxBlock, 4) trace_kernel(const TraceArg
                          ? (int)__reduce_max_sync(kFull, vx.conn ? (unsigned)st.num_recs : 0u)
                          : a.num_recs;
     for (int ri = 0; ri < nrec; ++ri) {
-      if (vx.conn && (MODE != kModeBatch || ri < st.num_recs) &&
-          connect_one<MODE>(a, s_scenes, st, vx, ri, c, err, s_first, s_last))
-        vis |= 1u << (ri & 31);
+      int res = kNotTested;
+      if (vx.conn && (MODE != kModeBatch || ri < st.num_recs))
+        res = connect_one<MODE>(a, s_scenes, st, vx, ri, c, err, s_first, s_last);
+      if (res == kVisible) vis |= 1u << (ri & 31);
       __syncwarp();
     }
     // phase 4: cut-off, next direction, bounce limit (src/Scene.cpp:275-277)
@@ -1024,6 +1031,35 @@ __global__ void __launch_bounds__(kTraceMaxBlock, 4) trace_kernel(const TraceArg
     if (s_last[i] > 0) atomicMax(&a.first_last[i].y, s_last[i]);
     if (s_first[i] < kInitialFirstSample) atomicMin(&a.first_last[i].x, s_first[i]);
   }
+}
+
+// Occlusion probe for the visibility order: n seeded segments from
+// triangle centroids, moved 1 mm off the surface on the side facing the
+// listener, to the render's recorders; counts the blocked ones.  Only the
+// traversal order of later visibility tests depends on the result.
+__global__ void occlusion_probe_kernel(const TraceArgs a, int n, unsigned* blocked) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || a.num_tris < 1 || a.num_recs < 1) return;
+  const U4 r = philox4x32_10((uint32_t)k, 0x9e3779b9u, 0u, 0u, 0x85ebca6bu, 0xc2b2ae35u);
+  const int i = (int)(r.x % (uint32_t)a.num_tris);
+  const DevRecorder& R = a.recs[r.y % (uint32_t)a.num_recs];
+  const float4* T = a.tris + 4 * i;
+  const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2), Nn = __ldg(T + 3);
+  const V3 c = mk(A.x + (B.x + C.x) / 3.0f, A.y + (B.y + C.y) / 3.0f, A.z + (B.z + C.z) / 3.0f);
+  const V3 rl = mk(R.loc[0], R.loc[1], R.loc[2]);
+  V3 nn = mk(Nn.x, Nn.y, Nn.z);
+  if (dot(nn, sub(rl, c)) < 0.0f) nn = neg(nn);
+  const V3 o = mk(c.x + nn.x * 1e-3f, c.y + nn.y * 1e-3f, c.z + nn.z * 1e-3f);
+  const V3 seg = sub(rl, o);
+  const float len = length(seg);
+  if (!(len > 0.0f)) return;
+  PathState st;
+  st.scene = 0;
+  const SceneRef S = scene_of<kModeForward>(a, nullptr, st);
+  LaneCounters cnt = {0, 0, 0, 0, 0, 0, 0};
+  int err = 0;
+  Hit h;
+  if (traverse<true>(S, o, seg, 1.0f, kSlackRel + S.box_pad / len, h, cnt, err)) atomicAdd(blocked, 1u);
 }
 
 }  // namespace EAR_NS

@@ -44,9 +44,14 @@ cudaError_t occ(int mode, int block, size_t smem, int* blocks_per_sm) {
   }
 }
 
+cudaError_t probe(const TraceArgs& a, int n, unsigned* blocked, cudaStream_t s) {
+  occlusion_probe_kernel<<<(n + 255) / 256, 256, 0, s>>>(a, n, blocked);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
-const TraceOps kOps = {trace, occ, kTraceMaxBlock};
+const TraceOps kOps = {trace, occ, probe, kTraceMaxBlock};
 
 }  // namespace EAR_NS
 }  // namespace ear

@@ -114,7 +114,13 @@ typedef struct ear_bvh_opts {
      4-wide from 4096 triangles on.  Both trees are built; the choice can
      be changed later with ear_scene_set_bvh_width.  Never changes a result. */
   int32_t width;
-  int32_t reserved[3];
+  /* Order of the visibility tests' traversal: 1 nearest hit child first, 2
+     farthest first (meets occluders between the surface and the listener
+     sooner), 0 = automatic: farthest first when a probe at build time
+     finds more than 15% of 8192 segments between triangle pairs blocked.
+     Never changes a result. */
+  int32_t visibility_order;
+  int32_t reserved[2];
 } ear_bvh_opts;
 
 #define EAR_BVH_DEFAULT 0
@@ -175,7 +181,8 @@ typedef struct ear_render_stats {
   uint64_t shadow_queries; /* any-hit (visibility) queries */
   uint64_t contributions;  /* valid recorded path contributions */
   uint64_t sampler_overflows; /* rejection loops that reached their bound */
-  uint64_t node_visits;    /* BVH internal-node visits (64 bytes each) */
+  uint64_t node_visits;    /* BVH node visits in 64-byte units (a 4-wide
+                              node counts 2) */
   uint64_t triangle_tests; /* ray/triangle tests (48 bytes each) */
   uint64_t splat_bins;     /* histogram bins written by splats */
   double kernel_ms;        /* device time of the trace kernel(s) */

@@ -84,7 +84,9 @@ def test_builders_find_the_same_hits():
     ref = None
     for builder, extra in [("lbvh", {}), ("ploc", {}), ("ploc", {"ploc_radius": 4}),
                            ("lbvh", {"max_leaf": 4}), ("lbvh", {"width": 4}),
-                           ("ploc", {"width": 4}), ("lbvh", {"max_leaf": 4, "width": 4})]:
+                           ("ploc", {"width": 4}), ("lbvh", {"max_leaf": 4, "width": 4}),
+                           ("ploc", {"width": 4, "visibility_order": 2}),
+                           ("ploc", {"width": 2, "visibility_order": 2})]:
         with Tracer(r.vertices, r.material_ids, r.materials, builder=builder, **extra) as tr:
             got = tr.trace_debug(r.sources[0], r.listeners, band=0, max_record=80, exact=True, **kw)
             info = tr.info()
