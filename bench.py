@@ -442,6 +442,12 @@ def run_ours(args):
     achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else 0.0
     hbm, src = peaks()
     per_launch = alg_bytes / args.steps
+    # DRAM traffic of the trace kernel per launch from one ncu capture of the
+    # default workload (profiles/dram_traffic_relief_hall_bench.md); other
+    # workloads and ray counts report null
+    traffic = None
+    if w.name == "relief-hall-20k-stereo" and int(kw["num_rays"]) == 10_000_000 and not exact:
+        traffic = 180_881_920
 
     # e2e through the C ABI from pinned host memory, every step
     e2e = None
@@ -499,7 +505,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
             "config": cfg,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm, "traffic": traffic,
                          "peak_source": src, "kernel": "trace_kernel<false>",
                          "algorithmic_bytes_per_launch": per_launch,
                          "kernel_ms_per_launch": kern_ms / args.steps},
