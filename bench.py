@@ -442,9 +442,9 @@ def run_ours(args):
     achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else 0.0
     hbm, src = peaks()
     per_launch = alg_bytes / args.steps
-    # DRAM traffic of the trace kernel per launch from one ncu capture of the
-    # default workload (profiles/dram_traffic_relief_hall_bench.md); other
-    # workloads and ray counts report null
+    # DRAM traffic of the trace kernel per launch, dram__bytes_read.sum +
+    # dram__bytes_write.sum from one ncu capture of this default workload
+    # (1e7 rays/band, fast kernels); other workloads report null
     traffic = None
     if w.name == "relief-hall-20k-stereo" and int(kw["num_rays"]) == 10_000_000 and not exact:
         traffic = 180_881_920
