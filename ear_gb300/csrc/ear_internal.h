@@ -19,10 +19,11 @@ struct __align__(32) Node {
   int4 d;    // child0 child1 parent depth
 };
 
-// 4-wide node, 128 bytes, built from the binary tree: the binary nodes at
-// even depth, each with the up to four grandchildren (or leaf children) of
-// its subtree as children.  Boxes per axis for the four slots; a child >= 0
-// is an internal Node4, < 0 a leaf code as in Node.
+// 4-wide node, 128 bytes, built top-down from the binary tree: a node's
+// children are the up to four subtrees left after repeatedly opening the
+// largest-area internal child of its binary node.  Boxes per axis for the
+// four slots; a child >= 0 is an internal Node4, < 0 a leaf code as in
+// Node.
 struct __align__(32) Node4 {
   float4 lox, hix, loy, hiy, loz, hiz;
   int4 child;

@@ -12,8 +12,10 @@
 // with one atomic per warp (ballot + popc + shuffle), so warps stay full
 // while path lengths vary from 1 to max_bounces.  Warps reconverge
 // (__syncwarp) after every data-dependent loop.  BVH traversal is
-// stackless: a 64-bit trail records, per level of the current root path,
-// whether the far child is still pending; backtracking climbs parent links.
+// stackless: over the binary tree a 64-bit trail records, per level of the
+// current root path, whether the far child is still pending; over the
+// 4-wide tree a 128-bit trail holds the mask of pending children per
+// level; backtracking climbs parent links.
 //
 // Batch mode (kModeBatch) runs the same loop over many jobs -- (scene,
 // source position, recorders) triples of a sweep over rooms, source /

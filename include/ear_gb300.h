@@ -183,7 +183,7 @@ typedef struct ear_render_stats {
   uint64_t sampler_overflows; /* rejection loops that reached their bound */
   uint64_t node_visits;    /* BVH node visits in 64-byte units (a 4-wide
                               node counts 2) */
-  uint64_t triangle_tests; /* ray/triangle tests (48 bytes each) */
+  uint64_t triangle_tests; /* ray/triangle tests (48 bytes of geometry each) */
   uint64_t splat_bins;     /* histogram bins written by splats */
   double kernel_ms;        /* device time of the trace kernel(s) */
 } ear_render_stats;
