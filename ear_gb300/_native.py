@@ -113,6 +113,23 @@ class EarTuneResult(C.Structure):
                 ("candidates", C.c_int32), ("from_cache", C.c_int32)]
 
 
+EAR_AURAL_DEVICE_MEMORY = 1
+EAR_CONV_FFT = 0
+EAR_CONV_DIRECT = 1
+
+
+class EarConvContext(C.Structure):
+    _fields_ = [("ir", C.c_void_p), ("ir_capacity", C.c_int64), ("ir_first", C.c_int64),
+                ("ir_length", C.c_int64), ("ir_next", C.c_void_p), ("ir_next_capacity", C.c_int64),
+                ("ir_next_first", C.c_int64), ("ir_next_length", C.c_int64), ("dry", C.c_void_p),
+                ("dry_length", C.c_int64), ("offset", C.c_int64)]
+
+
+class EarConvStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_float), ("launches", C.c_int32), ("fft_points", C.c_int64),
+                ("multiply_adds", C.c_double)]
+
+
 # Every exported symbol of include/ear_gb300.h with its ctypes signature.
 SIGNATURES = {
     "ear_last_error": (C.c_char_p, []),
@@ -160,6 +177,13 @@ SIGNATURES = {
     "ear_track_t60": (C.c_float, [C.c_void_p, C.c_int32, C.c_int32]),
     "ear_statistical_t60": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(EarMaterial),
                                       C.c_float, C.c_void_p]),
+    "ear_band_split": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
+    "ear_convolve": (C.c_int, [C.POINTER(EarConvContext), C.c_int32, C.c_int32, C.c_void_p,
+                               C.c_int64, C.c_uint32, C.c_void_p, C.c_int32,
+                               C.POINTER(EarConvStats)]),
+    "ear_conv_processed_capacity": (C.c_int64, [C.POINTER(EarConvContext), C.c_int32]),
+    "ear_conv_processed_length": (C.c_int64, [C.POINTER(EarConvContext), C.c_int32]),
 }
 
 _LIB = None

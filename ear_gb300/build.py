@@ -43,8 +43,10 @@ CUDA_UNITS = [
     ("trace_fast.cu", ["--fmad=true"]),
     ("api.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
+    # exact paths use explicit _rn intrinsics; the FFT may contract
+    ("aural.cu", ["--fmad=true"]),
 ]
-CLI_SOURCES = ["cli/ear_cli.cpp", "cli/earfile.cpp"]
+CLI_SOURCES = ["cli/ear_cli.cpp", "cli/earfile.cpp", "cli/wavefile.cpp"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,964 @@
+// aural.cu -- auralisation on the device: the equalizer band split of the
+// dry sounds and the convolution of the recorder tracks with them, the steps
+// of Render() after the impulse responses (src/EAR.cpp:295-386).
+//
+//  * Band split (Equalizer::Split, lib/equalizer/Equalizer.cpp:81-96): four
+//    IIR recurrences per signal.  Each output sample depends on the previous
+//    four, in FP32, so the filters run sequentially -- one thread per output
+//    chain (low, high, and mid = HP(LP(x))) -- with the reference's operation
+//    order (explicit _rn intrinsics, no contraction): bit-identical outputs.
+//  * Direct convolution (RecorderTrack::Process without FFTW,
+//    src/Recorder.cpp:247-292): out[x] = sum_i s_i * h(x - off - i), summed
+//    for each x in ascending i as the reference's loop nest does, then added
+//    to the recorder total context by context.  Register-blocked: a thread
+//    owns kDirR consecutive outputs and slides the response window through
+//    registers; dry and response chunks are staged in shared memory.  The
+//    sum order is the reference's, so the results are bit-identical.
+//  * FFT convolution (the FFTW build, src/Recorder.cpp:145-243): a
+//    hand-written radix-16 Stockham FFT (global-memory passes, L2-resident
+//    for these sizes).  The response and the dry section share one complex
+//    transform (response real, dry imaginary); the product of their spectra
+//    is separated from it, two contexts share one inverse transform.
+//    Keyframe pairs fade the section out under this keyframe's response and
+//    in under the next's, with the reference's sequential FP32 fade ramp.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/ear_gb300.h"
+#include "host_internal.h"
+
+namespace ear {
+namespace {
+
+// ------------------------------------------------------------- band split
+
+struct LrFilter {
+  float a0, a1, a2, a3, a4, b1, b2, b3, b4;
+};
+
+// Equalizer::Pass::Pass, LowPass::LowPass, HighPass::HighPass
+// (lib/equalizer/Equalizer.cpp:33-79): the same expressions in the same
+// order (host code, compiled without contraction); pi is the reference's
+// 3.14285714285714f.
+LrFilter lr_filter(float fc, bool high) {
+  const float srate = 44100.0f;
+  const float pi = 3.14285714285714f;
+  const float wc = 2.0f * pi * srate;
+  const float wc2 = wc * wc;
+  const float wc3 = wc2 * wc;
+  const float wc4 = wc2 * wc2;
+  const float k = wc / std::tan(pi * fc / srate);
+  const float k2 = k * k;
+  const float k3 = k2 * k;
+  const float k4 = k2 * k2;
+  const float sqrt2 = std::sqrt(2.0f);
+  const float sq_tmp1 = sqrt2 * wc3 * k;
+  const float sq_tmp2 = sqrt2 * wc * k3;
+  const float a_tmp = 4.0f * wc2 * k2 + 2.0f * sq_tmp1 + k4 + 2.0f * sq_tmp2 + wc4;
+  LrFilter f;
+  f.b1 = (4.0f * (wc4 + sq_tmp1 - k4 - sq_tmp2)) / a_tmp;
+  f.b2 = (6.0f * wc4 - 8.0f * wc2 * k2 + 6.0f * k4) / a_tmp;
+  f.b3 = (4.0f * (wc4 - sq_tmp1 + sq_tmp2 - k4)) / a_tmp;
+  f.b4 = (k4 - 2.0f * sq_tmp1 + wc4 - 2.0f * sq_tmp2 + 4.0f * wc2 * k2) / a_tmp;
+  if (high) {
+    f.a0 = k4 / a_tmp;
+    f.a1 = -4.0f * k4 / a_tmp;
+    f.a2 = 6.0f * k4 / a_tmp;
+  } else {
+    f.a0 = wc4 / a_tmp;
+    f.a1 = 4.0f * wc4 / a_tmp;
+    f.a2 = 6.0f * wc4 / a_tmp;
+  }
+  f.a3 = f.a1;
+  f.a4 = f.a0;
+  return f;
+}
+
+struct LrState {
+  float x1, x2, x3, x4, y1, y2, y3, y4;
+};
+
+// Equalizer::Pass::Process (lib/equalizer/Equalizer.cpp:26-31), evaluated
+// left to right as written.
+__device__ __forceinline__ float lr_step(const LrFilter& f, LrState& s, float in) {
+  float o = __fmul_rn(f.a0, in);
+  o = __fadd_rn(o, __fmul_rn(f.a1, s.x1));
+  o = __fadd_rn(o, __fmul_rn(f.a2, s.x2));
+  o = __fadd_rn(o, __fmul_rn(f.a3, s.x3));
+  o = __fadd_rn(o, __fmul_rn(f.a4, s.x4));
+  o = __fsub_rn(o, __fmul_rn(f.b1, s.y1));
+  o = __fsub_rn(o, __fmul_rn(f.b2, s.y2));
+  o = __fsub_rn(o, __fmul_rn(f.b3, s.y3));
+  o = __fsub_rn(o, __fmul_rn(f.b4, s.y4));
+  s.x4 = s.x3;
+  s.x3 = s.x2;
+  s.x2 = s.x1;
+  s.x1 = in;
+  s.y4 = s.y3;
+  s.y3 = s.y2;
+  s.y2 = s.y1;
+  s.y1 = o;
+  return o;
+}
+
+struct SplitArgs {
+  const float* x;
+  float* out[3];  // low, mid, high
+  int64_t n;
+  LrFilter lp1, lp2, hp1, hp2;  // crossovers 1 and 2
+};
+
+constexpr int kSplitBatch = 16;
+
+// Thread 0: low = LP1(x); thread 1: high = HP2(x); thread 2: mid =
+// HP1(LP2(x)).  Inputs are read in batches so the loads overlap the
+// recurrence.
+__global__ void k_band_split(SplitArgs a) {
+  const int c = threadIdx.x;
+  if (c > 2) return;
+  const LrFilter f0 = c == 0 ? a.lp1 : (c == 1 ? a.hp2 : a.lp2);
+  const LrFilter& f1 = a.hp1;
+  LrState s0 = {0, 0, 0, 0, 0, 0, 0, 0}, s1 = s0;
+  float* out = a.out[c == 0 ? 0 : (c == 1 ? 2 : 1)];
+  float buf[kSplitBatch];
+  for (int64_t t0 = 0; t0 < a.n; t0 += kSplitBatch) {
+    const int m = (int)(a.n - t0 < kSplitBatch ? a.n - t0 : kSplitBatch);
+#pragma unroll
+    for (int u = 0; u < kSplitBatch; ++u) buf[u] = u < m ? __ldg(a.x + t0 + u) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < kSplitBatch; ++u) {
+      if (u < m) {
+        float y = lr_step(f0, s0, buf[u]);
+        if (c == 2) y = lr_step(f1, s1, y);
+        out[t0 + u] = y;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------ direct convolution
+
+// One context as the direct kernel reads it.  h(j) is the response at j for
+// j in [first, len): ir[j] below cap, else 0; with a keyframe partner the
+// two responses are read raw over the joint [first, len) (as the reference
+// does, src/Recorder.cpp:276-289) and interpolated with i1 = i * inv_n.
+struct DirectCtx {
+  const float* ir;
+  const float* ir2;
+  const float* dry;
+  int64_t cap, cap2;
+  int64_t first, len;
+  int64_t n, off;
+  float inv_n;
+  int interp;
+};
+
+constexpr int kDirThreads = 128;
+constexpr int kDirR = 9;  // outputs per thread; odd, so the window loads are bank-conflict free
+constexpr int kDirTile = kDirThreads * kDirR;
+constexpr int kDirChunk = 28 * kDirR;  // dry samples staged per step
+constexpr int kDirWin = kDirTile + kDirChunk - 1;
+
+__device__ __forceinline__ float dir_h(const float* p, int64_t cap, int64_t j, int64_t lo,
+                                       int64_t hi) {
+  return (j >= lo && j < hi && j < cap) ? p[j] : 0.0f;
+}
+
+// Sum of one context over the block's tile into acc (from +0, ascending i).
+template <bool INTERP>
+__device__ __forceinline__ void direct_context(const DirectCtx& C, int64_t x0, int t, float* s_dry,
+                                               float* s_h, float* s_h2, float (&acc)[kDirR]) {
+  // dry indices that reach this tile
+  const int64_t ilo = max((int64_t)0, x0 - C.off - C.len + 1);
+  const int64_t ihi = min(C.n - 1, x0 + kDirTile - 1 - C.off - C.first);
+  for (int64_t i0 = ilo; i0 <= ihi; i0 += kDirChunk) {
+    __syncthreads();
+    for (int k = t; k < kDirChunk; k += kDirThreads) {
+      const int64_t i = i0 + k;
+      s_dry[k] = i < C.n ? C.dry[i] : 0.0f;
+    }
+    // response window: s_h[w] = h(jb + w)
+    const int64_t jb = x0 - C.off - i0 - (kDirChunk - 1);
+    for (int w = t; w < kDirWin; w += kDirThreads) {
+      const int64_t j = jb + w;
+      s_h[w] = dir_h(C.ir, C.cap, j, C.first, C.len);
+      if (INTERP) s_h2[w] = dir_h(C.ir2, C.cap2, j, C.first, C.len);
+    }
+    __syncthreads();
+    // output r of the thread at step k reads s_h[wb + r - k]; the value for
+    // index v = r - k sits in register slot v mod kDirR, so one new value is
+    // loaded per step and nothing moves
+    const int wb = t * kDirR + kDirChunk - 1;
+    float hw[kDirR], hw2[kDirR];
+#pragma unroll
+    for (int r = 0; r < kDirR; ++r) {
+      hw[r] = s_h[wb + r];
+      hw2[r] = INTERP ? s_h2[wb + r] : 0.0f;
+    }
+    for (int k0 = 0; k0 < kDirChunk; k0 += kDirR) {
+#pragma unroll
+      for (int u = 0; u < kDirR; ++u) {
+        const int k = k0 + u;
+        const float s = s_dry[k];
+        if (INTERP) {
+          // i1 = i * flt_samples, i2 = 1 - i1 (src/Recorder.cpp:277-278)
+          const float i1 = __fmul_rn(__uint2float_rn((unsigned)(i0 + k)), C.inv_n);
+          const float i2 = __fsub_rn(1.0f, i1);
+#pragma unroll
+          for (int r = 0; r < kDirR; ++r) {
+            const int q = (r - u + kDirR) % kDirR;
+            const float p = __fadd_rn(__fmul_rn(i2, hw[q]), __fmul_rn(i1, hw2[q]));
+            acc[r] = __fadd_rn(acc[r], __fmul_rn(s, p));
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < kDirR; ++r) {
+            const int q = (r - u + kDirR) % kDirR;
+            acc[r] = __fadd_rn(acc[r], __fmul_rn(s, hw[q]));
+          }
+        }
+        // the slot of index kDirR-1-k leaves; index -k-1 enters
+        const int qn = (kDirR - 1 - u) % kDirR;
+        const int wn = wb - k - 1;
+        if (wn >= 0) {
+          hw[qn] = s_h[wn];
+          if (INTERP) hw2[qn] = s_h2[wn];
+        }
+      }
+    }
+  }
+}
+
+// One block: kDirTile consecutive outputs.  For each context in order its
+// own sum t[x] is accumulated from +0 in ascending i and then added to the
+// total, as RecorderTrack::Process and Recorder::Add do.  Terms outside a
+// context's range read zero-padded dry or response samples and add +-0,
+// which leaves every partial sum unchanged.  ANY_INTERP compiles the
+// keyframe-interpolation path in as well.
+template <bool ANY_INTERP>
+__global__ void __launch_bounds__(kDirThreads) k_conv_direct(const DirectCtx* __restrict__ ctxs,
+                                                             int num_ctx, float* __restrict__ out,
+                                                             int64_t out_len) {
+  __shared__ float s_dry[kDirChunk];
+  __shared__ float s_h[kDirWin];
+  __shared__ float s_h2[ANY_INTERP ? kDirWin : 1];
+  const int t = threadIdx.x;
+  const int64_t x0 = (int64_t)blockIdx.x * kDirTile;
+  const int64_t xt = x0 + (int64_t)t * kDirR;
+  float total[kDirR];
+#pragma unroll
+  for (int r = 0; r < kDirR; ++r) total[r] = xt + r < out_len ? out[xt + r] : 0.0f;
+  for (int c = 0; c < num_ctx; ++c) {
+    const DirectCtx C = ctxs[c];
+    if (C.len <= C.first || C.n <= 0) continue;
+    if (x0 + kDirTile - 1 < C.off + C.first || x0 > C.off + C.n - 1 + C.len - 1) continue;
+    float acc[kDirR];
+#pragma unroll
+    for (int r = 0; r < kDirR; ++r) acc[r] = 0.0f;
+    if (ANY_INTERP && C.interp)
+      direct_context<true>(C, x0, t, s_dry, s_h, s_h2, acc);
+    else
+      direct_context<false>(C, x0, t, s_dry, s_h, s_h2, acc);
+#pragma unroll
+    for (int r = 0; r < kDirR; ++r) total[r] = __fadd_rn(total[r], acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < kDirR; ++r)
+    if (xt + r < out_len) out[xt + r] = total[r];
+}
+
+// --------------------------------------------------------- FFT convolution
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// exp(-2 pi i m / 2^log2n).  The argument of sincospif is exact for
+// 2^log2n <= 2^24; above that the angle is split into a coarse and a fine
+// factor.
+__device__ __forceinline__ float2 twiddle(uint32_t m, int log2n) {
+  float s, c;
+  if (log2n <= 24) {
+    sincospif(ldexpf((float)m, 1 - log2n), &s, &c);
+    return make_float2(c, -s);
+  }
+  const uint32_t hi = m >> 12, lo = m & 4095u;
+  float s2, c2;
+  sincospif(ldexpf((float)hi, 13 - log2n), &s, &c);
+  sincospif(ldexpf((float)lo, 1 - log2n), &s2, &c2);
+  return cmul(make_float2(c, -s), make_float2(c2, -s2));
+}
+
+// exp(-2 pi i q / 16), q in [0, 8)
+__device__ __forceinline__ float2 w16(int q) {
+  constexpr float c1 = 0.923879532511286756f, s1 = 0.382683432365089772f;
+  constexpr float h = 0.707106781186547524f;
+  switch (q) {
+    case 0: return make_float2(1.0f, 0.0f);
+    case 1: return make_float2(c1, -s1);
+    case 2: return make_float2(h, -h);
+    case 3: return make_float2(s1, -c1);
+    case 4: return make_float2(0.0f, -1.0f);
+    case 5: return make_float2(-s1, -c1);
+    case 6: return make_float2(-h, -h);
+    default: return make_float2(-c1, -s1);
+  }
+}
+
+template <int R>
+__device__ __forceinline__ int bitrev(int i) {
+  int r = 0;
+#pragma unroll
+  for (int b = 1; b < R; b <<= 1) {
+    r = (r << 1) | (i & 1);
+    i >>= 1;
+  }
+  return r;
+}
+
+// In-register DFT of size R (2, 4, 8 or 16), natural order in and out:
+// iterative radix-2 decimation in time.
+template <int R>
+__device__ __forceinline__ void dft(float2 (&a)[R]) {
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int j = bitrev<R>(i);
+    if (j > i) {
+      const float2 t = a[i];
+      a[i] = a[j];
+      a[j] = t;
+    }
+  }
+#pragma unroll
+  for (int m = 1; m < R; m <<= 1) {
+#pragma unroll
+    for (int k = 0; k < m; ++k) {
+      const float2 w = w16(k * (16 / (2 * m)));
+#pragma unroll
+      for (int i = k; i < R; i += 2 * m) {
+        const float2 u = a[i];
+        const float2 v = k == 0 ? a[i + m] : cmul(a[i + m], w);
+        a[i] = cadd(u, v);
+        a[i + m] = csub(u, v);
+      }
+    }
+  }
+}
+
+// One radix-R Stockham pass over every slot of a group (blockIdx.y = slot):
+// combines R sub-transforms of size 2^log2ns into one of size 2^log2ns * R.
+// After passes with sub-sizes 1, R1, R1*R2, ... the output is in natural
+// order.
+template <int R>
+__global__ void __launch_bounds__(256) k_fft_pass(const float2* __restrict__ in,
+                                                  float2* __restrict__ out, int log2l, int log2ns) {
+  constexpr int kLogR = R == 2 ? 1 : (R == 4 ? 2 : (R == 8 ? 3 : 4));
+  const int64_t l = (int64_t)1 << log2l;
+  const int64_t stride = l / R;  // threads per slot
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= stride) return;
+  const int64_t base = (int64_t)blockIdx.y * l;
+  float2 a[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) a[r] = in[base + j + r * stride];
+  const int64_t ns = (int64_t)1 << log2ns;
+  const int64_t jm = j & (ns - 1);
+  if (log2ns > 0) {
+#pragma unroll
+    for (int r = 1; r < R; ++r) a[r] = cmul(a[r], twiddle((uint32_t)(jm * r), log2ns + kLogR));
+  }
+  dft<R>(a);
+  const int64_t d = ((j >> log2ns) << (log2ns + kLogR)) + jm;
+#pragma unroll
+  for (int r = 0; r < R; ++r) out[base + d + r * ns] = a[r];
+}
+
+// Input slot of a group: z[t] = h(t) + i * s(t) * fade(t), h read over
+// [0, m) (zero from cap on), s over [0, n).
+struct FftSlot {
+  const float* ir;
+  const float* dry;
+  const float* fade;  // null: no fade
+  int64_t cap, m, n;
+};
+
+__global__ void k_fft_pack(const FftSlot* __restrict__ slots, float2* __restrict__ z, int log2l) {
+  const int64_t l = (int64_t)1 << log2l;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= l) return;
+  const FftSlot S = slots[blockIdx.y];
+  float re = 0.0f, im = 0.0f;
+  if (t < S.m && t < S.cap) re = S.ir[t];
+  if (t < S.n) im = S.fade ? __fmul_rn(S.dry[t], S.fade[t]) : S.dry[t];
+  z[(int64_t)blockIdx.y * l + t] = make_float2(re, im);
+}
+
+// RecorderTrack::Process with a fade (src/Recorder.cpp:168-179): factor
+// starts at 1 (fade out) or 0 (fade in) and steps by -+1/n in FP32, in
+// sequence -- the ramp is the reference's rounded one, not an exact line.
+// One thread per ramp.
+struct FadeRamp {
+  float* out;
+  int64_t n;
+  int fade_in;
+};
+
+__global__ void k_fade_ramp(const FadeRamp* __restrict__ ramps, int num) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= num) return;
+  const FadeRamp R = ramps[r];
+  float factor = R.fade_in ? 0.0f : 1.0f;
+  const float df = __fdiv_rn(R.fade_in ? 1.0f : -1.0f, (float)R.n);
+  for (int64_t i = 0; i < R.n; ++i) {
+    R.out[i] = factor;
+    factor = __fadd_rn(factor, df);
+  }
+}
+
+// Spectrum product of up to two contexts sharing one inverse transform.
+// Z = H + iD of a slot gives H = (Z[k] + conj Z[-k]) / 2 and
+// D = (Z[k] - conj Z[-k]) / 2i; a context's spectrum is the sum over its
+// one or two slots of H * D.  W = conj(Y_a + i Y_b) / l, so the forward
+// transform of W is y_a - i y_b.
+struct FftPair {
+  int a0, a1, b0, b1;  // slots; -1 = none
+};
+
+__device__ __forceinline__ float2 slot_product(const float2* z, int64_t l, int s, int64_t k,
+                                               int64_t kn) {
+  const float2 zk = z[(int64_t)s * l + k];
+  const float2 zn = z[(int64_t)s * l + kn];
+  const float2 h = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+  // (zk - conj zn) / 2i
+  const float2 dd = make_float2(0.5f * (zk.x - zn.x), 0.5f * (zk.y + zn.y));
+  const float2 d = make_float2(dd.y, -dd.x);
+  return cmul(h, d);
+}
+
+__global__ void k_fft_product(const float2* __restrict__ z, const FftPair* __restrict__ pairs,
+                              float2* __restrict__ w, int log2l) {
+  const int64_t l = (int64_t)1 << log2l;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= l) return;
+  const FftPair P = pairs[blockIdx.y];
+  const int64_t kn = (l - k) & (l - 1);
+  float2 ya = slot_product(z, l, P.a0, k, kn);
+  if (P.a1 >= 0) ya = cadd(ya, slot_product(z, l, P.a1, k, kn));
+  float2 yb = make_float2(0.0f, 0.0f);
+  if (P.b0 >= 0) {
+    yb = slot_product(z, l, P.b0, k, kn);
+    if (P.b1 >= 0) yb = cadd(yb, slot_product(z, l, P.b1, k, kn));
+  }
+  const float inv = 1.0f / (float)l;  // exact: l is a power of two
+  // y = ya + i yb; w = conj(y) / l
+  w[(int64_t)blockIdx.y * l + k] = make_float2((ya.x - yb.y) * inv, -(ya.y + yb.x) * inv);
+}
+
+// Processed track of one context: v[x] (real part) or -v[x] (imaginary
+// part) of its pair's inverse, for x in [0, mn), landing at off + x.
+struct FftOut {
+  const float2* v;
+  int64_t off, mn;
+  int imag;
+};
+
+__global__ void k_fft_accumulate(const FftOut* __restrict__ outs, int num, float* __restrict__ out,
+                                 int64_t x0, int64_t x1) {
+  const int64_t x = x0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= x1) return;
+  float acc = out[x];
+  for (int c = 0; c < num; ++c) {
+    const FftOut O = outs[c];
+    const int64_t u = x - O.off;
+    if (u < 0 || u >= O.mn) continue;
+    const float2 v = O.v[u];
+    acc += O.imag ? -v.y : v.x;
+  }
+  out[x] = acc;
+}
+
+// ------------------------------------------------------------ host side
+
+constexpr int64_t kInitialCapacity = 3 * 44100;  // INITIAL_BUFFER_SIZE, src/Recorder.h:36
+constexpr int64_t kIncrement = 44100;            // INCREMENTAL_BUFFER_SIZE, src/Recorder.h:37
+
+// FloatBuffer capacity after writes that start at index a and then never
+// jump more than one past the highest index so far, up to b
+// (FloatBuffer::operator[], src/Recorder.cpp:52-59).
+int64_t grown(int64_t cap, int64_t a, int64_t b) {
+  if (b < a) return cap;
+  if (a >= cap) cap = a + kIncrement;
+  if (b >= cap) cap += kIncrement * ((b - cap) / kIncrement + 1);
+  return cap;
+}
+
+// Device scratch, grown on demand and kept per device.
+struct Scratch {
+  std::mutex mu;
+  char* buf = nullptr;
+  size_t cap = 0;
+  char* tab = nullptr;  // small tables
+  size_t tab_cap = 0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+Scratch& scratch(int device) {
+  static Scratch s[64];
+  return s[device & 63];
+}
+
+cudaError_t ensure(char** p, size_t* cap, size_t n) {
+  if (*cap >= n && *p) return cudaSuccess;
+  const size_t want = std::max(n, *cap + *cap / 2);
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void**)p, want);
+  if (e == cudaSuccess) *cap = want;
+  return e;
+}
+
+int log2_ceil(int64_t v) {
+  int l = 0;
+  while (((int64_t)1 << l) < v) ++l;
+  return l;
+}
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+bool check_context(const ear_conv_context& c, int i) {
+  if (c.dry_length < 0 || c.offset < 0 || c.ir_capacity < 0 || c.ir_first < 0 || c.ir_length < 0) {
+    fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d has a negative size or offset", i);
+    return false;
+  }
+  if ((c.dry_length > 0 && !c.dry) || (c.ir_capacity > 0 && !c.ir)) {
+    fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d has a null buffer", i);
+    return false;
+  }
+  if (c.ir_next && (c.ir_next_capacity < 0 || c.ir_next_first < 0 || c.ir_next_length < 0)) {
+    fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d has a negative next-keyframe size", i);
+    return false;
+  }
+  if (c.dry_length > 0x7fffffffLL || c.ir_length > 0x7fffffffLL || c.ir_next_length > 0x7fffffffLL) {
+    fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d exceeds 2^31 samples", i);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+}  // namespace ear
+
+using namespace ear;
+
+extern "C" {
+
+int64_t ear_conv_processed_capacity(const ear_conv_context* c, int32_t mode) {
+  if (!c) return kInitialCapacity;
+  const int64_t n = c->dry_length, off = c->offset;
+  if (mode == EAR_CONV_DIRECT) {
+    int64_t first = c->ir_first, len = c->ir_length;
+    if (c->ir_next) {
+      first = std::min(first, c->ir_next_first);
+      len = std::max(len, c->ir_next_length);
+    }
+    if (n <= 0 || len <= first) return kInitialCapacity;
+    return grown(kInitialCapacity, off + first, off + (n - 1) + (len - 1));
+  }
+  // FFT: c[i] written to off + i for i < M + N + 1
+  const int64_t ca = grown(kInitialCapacity, off, off + c->ir_length + n);
+  if (!c->ir_next) return ca;
+  const int64_t cb = grown(kInitialCapacity, off, off + c->ir_next_length + n);
+  // a->Add(b) reads b over its capacity (src/Recorder.cpp:294-299)
+  return grown(ca, 0, cb - 1);
+}
+
+int64_t ear_conv_processed_length(const ear_conv_context* c, int32_t mode) {
+  if (!c) return 0;
+  const int64_t n = c->dry_length, off = c->offset;
+  if (mode == EAR_CONV_DIRECT) {
+    int64_t first = c->ir_first, len = c->ir_length;
+    if (c->ir_next) {
+      first = std::min(first, c->ir_next_first);
+      len = std::max(len, c->ir_next_length);
+    }
+    if (n <= 0 || len <= first) return 0;
+    return off + (n - 1) + (len - 1);
+  }
+  const int64_t ra = off + c->ir_length + n;  // last of off + [0, M + N + 1)
+  if (!c->ir_next) return ra;
+  const int64_t cb = grown(kInitialCapacity, off, off + c->ir_next_length + n);
+  return std::max(ra, cb - 1);
+}
+
+ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3], float* low,
+                          float* mid, float* high, uint32_t flags, void* stream, int32_t device) {
+  if (n < 0 || !freq_khz) return fail(EAR_ERR_INVALID_ARG, "ear_band_split: bad arguments");
+  if (n > 0 && (!dry || !low || !mid || !high))
+    return fail(EAR_ERR_INVALID_ARG, "ear_band_split: null buffer");
+  for (int i = 0; i < 3; ++i)
+    if (!(freq_khz[i] > 0.0f) || !(freq_khz[i] * 1000.0f < 22050.0f))
+      return fail(EAR_ERR_INVALID_ARG, "ear_band_split: band frequency %d out of (0, 22.05) kHz", i);
+  if (n == 0) return EAR_OK;
+  CU(cudaSetDevice(device));
+  // SoundFile::Band multiplies by 1000, Equalizer::Split averages
+  // neighbours (src/SoundFile.cpp:153, lib/equalizer/Equalizer.cpp:84-85)
+  const float f1 = freq_khz[0] * 1000.0f, f2 = freq_khz[1] * 1000.0f, f3 = freq_khz[2] * 1000.0f;
+  const float fc1 = (f1 + f2) / 2.0f, fc2 = (f2 + f3) / 2.0f;
+  SplitArgs a;
+  a.lp1 = lr_filter(fc1, false);
+  a.lp2 = lr_filter(fc2, false);
+  a.hp1 = lr_filter(fc1, true);
+  a.hp2 = lr_filter(fc2, true);
+  a.n = n;
+  const bool on_dev = flags & EAR_AURAL_DEVICE_MEMORY;
+  cudaStream_t s = on_dev ? (cudaStream_t)stream : nullptr;
+  Scratch& sc = scratch(device);
+  std::lock_guard<std::mutex> lock(sc.mu);
+  if (on_dev) {
+    a.x = dry;
+    a.out[0] = low;
+    a.out[1] = mid;
+    a.out[2] = high;
+  } else {
+    CU(ensure(&sc.buf, &sc.cap, sizeof(float) * 4 * (size_t)n));
+    float* d = (float*)sc.buf;
+    CU(cudaMemcpyAsync(d, dry, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    a.x = d;
+    a.out[0] = d + n;
+    a.out[1] = d + 2 * n;
+    a.out[2] = d + 3 * n;
+  }
+  k_band_split<<<1, 32, 0, s>>>(a);
+  CU(cudaGetLastError());
+  if (!on_dev) {
+    CU(cudaMemcpyAsync(low, a.out[0], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(mid, a.out[1], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(high, a.out[2], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  }
+  CU(cudaStreamSynchronize(s));
+  return EAR_OK;
+}
+
+ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t mode, float* out,
+                        int64_t out_length, uint32_t flags, void* stream, int32_t device,
+                        ear_conv_stats* stats) {
+  if (stats) std::memset(stats, 0, sizeof *stats);
+  if (num < 0 || (num > 0 && !contexts) || out_length < 0 || (out_length > 0 && !out))
+    return fail(EAR_ERR_INVALID_ARG, "ear_convolve: bad arguments");
+  if (mode != EAR_CONV_FFT && mode != EAR_CONV_DIRECT)
+    return fail(EAR_ERR_INVALID_ARG, "ear_convolve: unknown mode %d", mode);
+  for (int i = 0; i < num; ++i)
+    if (!check_context(contexts[i], i)) return EAR_ERR_INVALID_ARG;
+  if (num == 0 || out_length == 0) return EAR_OK;
+  CU(cudaSetDevice(device));
+  const bool on_dev = flags & EAR_AURAL_DEVICE_MEMORY;
+  cudaStream_t s = on_dev ? (cudaStream_t)stream : nullptr;
+  Scratch& sc = scratch(device);
+  std::lock_guard<std::mutex> lock(sc.mu);
+  if (!sc.ev[0]) {
+    CU(cudaEventCreate(&sc.ev[0]));
+    CU(cudaEventCreate(&sc.ev[1]));
+  }
+
+  // ---- stage the caller's buffers (host calls): one device arena, each
+  // distinct host buffer copied once (a response serves as this keyframe's
+  // and the previous keyframe's partner; a band serves every recorder)
+  std::vector<ear_conv_context> ctx(contexts, contexts + num);
+  size_t staged = 0;
+  auto ir_need = [](const ear_conv_context& c) {
+    return std::max(c.ir_length, c.ir_next ? c.ir_next_length : (int64_t)0);
+  };
+  std::map<const float*, int64_t> spans;  // host buffer -> samples to copy
+  std::map<const float*, size_t> at;      // host buffer -> arena offset
+  if (!on_dev) {
+    auto want = [&spans](const float* p, int64_t n) {
+      if (!p || n <= 0) return;
+      int64_t& v = spans[p];
+      v = std::max(v, n);
+    };
+    for (int i = 0; i < num; ++i) {
+      const ear_conv_context& c = ctx[i];
+      want(c.ir, std::min(c.ir_capacity, ir_need(c)));
+      if (c.ir_next) want(c.ir_next, std::min(c.ir_next_capacity, ir_need(c)));
+      want(c.dry, c.dry_length);
+    }
+    for (const auto& kv : spans) {
+      at[kv.first] = staged;
+      staged += align256(sizeof(float) * (size_t)kv.second);
+    }
+    staged += align256(sizeof(float) * out_length);
+  }
+
+  // ---- mode-specific scratch layout
+  struct Group {
+    int log2l;
+    std::vector<int> jobs;  // context indices in order
+    int slots = 0, pairs = 0;
+    size_t at_a = 0, at_b = 0;
+  };
+  std::vector<Group> groups;
+  std::vector<int> slot0(num, -1), nslot(num, 0);
+  size_t fft_bytes = 0, ramp_bytes = 0;
+  std::vector<size_t> at_ramp(num, 0);
+  if (mode == EAR_CONV_FFT) {
+    for (int i = 0; i < num; ++i) {
+      const ear_conv_context& c = ctx[i];
+      int64_t mn = c.ir_length + c.dry_length + 1;
+      if (c.ir_next) mn = std::max(mn, c.ir_next_length + c.dry_length + 1);
+      const int lg = std::max(4, log2_ceil(mn));
+      if (lg > 30) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d needs a 2^%d transform", i, lg);
+      auto it = std::find_if(groups.begin(), groups.end(), [&](const Group& g) { return g.log2l == lg; });
+      if (it == groups.end()) {
+        groups.push_back(Group{lg, {}, 0, 0, 0, 0});
+        it = groups.end() - 1;
+      }
+      it->jobs.push_back(i);
+      nslot[i] = c.ir_next ? 2 : 1;
+      if (c.ir_next && c.dry_length > 0) {
+        at_ramp[i] = ramp_bytes;
+        ramp_bytes += align256(sizeof(float) * 2 * (size_t)c.dry_length);
+      }
+    }
+    for (Group& g : groups) {
+      for (int i : g.jobs) {
+        slot0[i] = g.slots;
+        g.slots += nslot[i];
+      }
+      g.pairs = ((int)g.jobs.size() + 1) / 2;
+      const size_t l = (size_t)1 << g.log2l;
+      g.at_a = fft_bytes;
+      fft_bytes += align256(sizeof(float2) * l * (size_t)g.slots);
+      g.at_b = fft_bytes;
+      fft_bytes += align256(sizeof(float2) * l * (size_t)std::max(g.slots, g.pairs));
+    }
+  }
+  const size_t total_bytes = staged + ramp_bytes + fft_bytes;
+  if (total_bytes > 0) CU(ensure(&sc.buf, &sc.cap, total_bytes));
+  char* arena = sc.buf;
+  float* d_out = out;
+  if (!on_dev) {
+    for (const auto& kv : spans)
+      CU(cudaMemcpyAsync(arena + at[kv.first], kv.first, sizeof(float) * kv.second,
+                         cudaMemcpyHostToDevice, s));
+    auto dev = [&](const float* p) { return p && at.count(p) ? (const float*)(arena + at[p]) : nullptr; };
+    for (int i = 0; i < num; ++i) {
+      ear_conv_context& c = ctx[i];
+      c.ir_capacity = c.ir ? std::min(c.ir_capacity, ir_need(c)) : 0;
+      c.ir = dev(c.ir);
+      if (c.ir_next) {
+        c.ir_next_capacity = std::min(c.ir_next_capacity, ir_need(c));
+        c.ir_next = dev(c.ir_next);
+        if (!c.ir_next) {  // nothing to read: keep the context a keyframe pair
+          c.ir_next = c.ir ? c.ir : (const float*)arena;
+          c.ir_next_capacity = 0;
+        }
+      }
+      if (!c.ir) c.ir_capacity = 0;
+      c.dry = dev(c.dry);
+    }
+    d_out = (float*)(arena + staged - align256(sizeof(float) * out_length));
+    CU(cudaMemcpyAsync(d_out, out, sizeof(float) * out_length, cudaMemcpyHostToDevice, s));
+  }
+  char* fft_arena = arena + staged + ramp_bytes;
+  float* ramps = (float*)(arena + staged);
+
+  // ---- small tables: one host block, one copy
+  std::vector<char> tab;
+  auto push = [&tab](const void* p, size_t bytes) {
+    const size_t at = align256(tab.size());
+    tab.resize(at + bytes);
+    if (bytes) std::memcpy(tab.data() + at, p, bytes);
+    return at;
+  };
+  int launches = 0;
+  double macs = 0;
+  int64_t points = 0;
+  CU(cudaEventRecord(sc.ev[0], s));
+  if (mode == EAR_CONV_DIRECT) {
+    std::vector<DirectCtx> dc(num);
+    bool any_interp = false;
+    for (int i = 0; i < num; ++i) {
+      const ear_conv_context& c = ctx[i];
+      DirectCtx& d = dc[i];
+      d.ir = c.ir;
+      d.ir2 = c.ir_next;
+      d.dry = c.dry;
+      d.cap = c.ir ? c.ir_capacity : 0;
+      d.cap2 = c.ir_next ? c.ir_next_capacity : 0;
+      d.first = c.ir_next ? std::min(c.ir_first, c.ir_next_first) : c.ir_first;
+      d.len = c.ir_next ? std::max(c.ir_length, c.ir_next_length) : c.ir_length;
+      d.n = c.dry_length;
+      d.off = c.offset;
+      d.inv_n = c.dry_length > 0 ? 1.0f / (float)(uint32_t)c.dry_length : 0.0f;
+      d.interp = c.ir_next ? 1 : 0;
+      any_interp |= d.interp != 0;
+      if (d.len > d.first && d.n > 0) macs += (double)d.n * (double)(d.len - d.first + kDirTile);
+    }
+    const size_t at = push(dc.data(), sizeof(DirectCtx) * num);
+    CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
+    CU(cudaMemcpyAsync(sc.tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
+    const DirectCtx* d_ctx = (const DirectCtx*)(sc.tab + at);
+    const int64_t blocks = (out_length + kDirTile - 1) / kDirTile;
+    if (blocks > 0x7fffffffLL) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output too long");
+    if (any_interp)
+      k_conv_direct<true><<<(unsigned)blocks, kDirThreads, 0, s>>>(d_ctx, num, d_out, out_length);
+    else
+      k_conv_direct<false><<<(unsigned)blocks, kDirThreads, 0, s>>>(d_ctx, num, d_out, out_length);
+    ++launches;
+    CU(cudaGetLastError());
+  } else {
+    // fade ramps of keyframe pairs
+    std::vector<FadeRamp> fr;
+    for (int i = 0; i < num; ++i) {
+      const ear_conv_context& c = ctx[i];
+      if (!c.ir_next || c.dry_length <= 0) continue;
+      float* r = (float*)((char*)ramps + at_ramp[i]);
+      fr.push_back(FadeRamp{r, c.dry_length, 0});
+      fr.push_back(FadeRamp{r + c.dry_length, c.dry_length, 1});
+    }
+    size_t at_fr = 0;
+    if (!fr.empty()) at_fr = push(fr.data(), sizeof(FadeRamp) * fr.size());
+    // per group: slots, pairs; then the outputs in context order
+    std::vector<size_t> at_slots(groups.size()), at_pairs(groups.size());
+    std::vector<FftOut> outs(num);
+    std::vector<int> final_in_a(groups.size());
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      Group& g = groups[gi];
+      std::vector<FftSlot> slots(g.slots);
+      for (int i : g.jobs) {
+        const ear_conv_context& c = ctx[i];
+        const float* ra = c.ir_next && c.dry_length > 0 ? (float*)((char*)ramps + at_ramp[i]) : nullptr;
+        FftSlot& a = slots[slot0[i]];
+        a = FftSlot{c.ir, c.dry, ra, c.ir ? c.ir_capacity : 0, c.ir_length, c.dry_length};
+        if (c.ir_next) {
+          slots[slot0[i] + 1] = FftSlot{c.ir_next, c.dry, ra ? ra + c.dry_length : nullptr,
+                                        c.ir_next_capacity, c.ir_next_length, c.dry_length};
+        }
+      }
+      std::vector<FftPair> pairs(g.pairs);
+      for (int p = 0; p < g.pairs; ++p) {
+        const int ia = g.jobs[2 * p];
+        const int ib = 2 * p + 1 < (int)g.jobs.size() ? g.jobs[2 * p + 1] : -1;
+        FftPair& P = pairs[p];
+        P.a0 = slot0[ia];
+        P.a1 = nslot[ia] == 2 ? slot0[ia] + 1 : -1;
+        P.b0 = ib >= 0 ? slot0[ib] : -1;
+        P.b1 = ib >= 0 && nslot[ib] == 2 ? slot0[ib] + 1 : -1;
+      }
+      at_slots[gi] = push(slots.data(), sizeof(FftSlot) * slots.size());
+      at_pairs[gi] = push(pairs.data(), sizeof(FftPair) * pairs.size());
+    }
+    const size_t at_outs_placeholder = push(outs.data(), sizeof(FftOut) * num);
+    CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
+    char* dtab = sc.tab;
+    if (!fr.empty()) {
+      // copied with the rest below; launched after the copy
+    }
+    // run the groups; the inverse of each pair ends in buffer a or b
+    std::vector<float2*> pair_result(groups.size());
+    auto passes = [&](float2* x, float2* y, int log2l, int count) -> float2* {
+      // radix-16 passes, then one of radix 2/4/8 for the remaining bits
+      int ns = 0;
+      float2* in = x;
+      float2* o = y;
+      const int64_t l = (int64_t)1 << log2l;
+      while (ns < log2l) {
+        const int rem = log2l - ns;
+        const int lr = rem >= 4 ? 4 : rem;
+        const int64_t thr = l >> lr;
+        dim3 grid((unsigned)((thr + 255) / 256), (unsigned)count);
+        switch (lr) {
+          case 4: k_fft_pass<16><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
+          case 3: k_fft_pass<8><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
+          case 2: k_fft_pass<4><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
+          default: k_fft_pass<2><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
+        }
+        ++launches;
+        ns += lr;
+        std::swap(in, o);
+      }
+      return in;  // holds the result
+    };
+    // the output table needs the result buffers, known only after planning
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      Group& g = groups[gi];
+      float2* A = (float2*)(fft_arena + g.at_a);
+      float2* B = (float2*)(fft_arena + g.at_b);
+      const int lg = g.log2l;
+      const int npass = (lg + 3) / 4;
+      // forward: A -> ... ; product into the other buffer; inverse back
+      float2* fwd = (npass % 2) ? B : A;
+      float2* prod = fwd == A ? B : A;
+      const int ninv = npass;
+      float2* inv = (ninv % 2) ? (prod == A ? B : A) : prod;
+      pair_result[gi] = inv;
+      const int64_t l = (int64_t)1 << lg;
+      points += l * (int64_t)(g.slots + g.pairs);
+      for (int p = 0; p < g.pairs; ++p) {
+        const int ia = g.jobs[2 * p];
+        outs[ia] = FftOut{inv + (int64_t)p * l, ctx[ia].offset,
+                          std::max(ctx[ia].ir_length, ctx[ia].ir_next ? ctx[ia].ir_next_length : 0) +
+                              ctx[ia].dry_length + 1,
+                          0};
+        if (2 * p + 1 < (int)g.jobs.size()) {
+          const int ib = g.jobs[2 * p + 1];
+          outs[ib] = FftOut{inv + (int64_t)p * l, ctx[ib].offset,
+                            std::max(ctx[ib].ir_length, ctx[ib].ir_next ? ctx[ib].ir_next_length : 0) +
+                                ctx[ib].dry_length + 1,
+                            1};
+        }
+      }
+    }
+    std::memcpy(tab.data() + at_outs_placeholder, outs.data(), sizeof(FftOut) * num);
+    CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
+    if (!fr.empty()) {
+      k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, s>>>((const FadeRamp*)(dtab + at_fr), (int)fr.size());
+      ++launches;
+    }
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      Group& g = groups[gi];
+      float2* A = (float2*)(fft_arena + g.at_a);
+      float2* B = (float2*)(fft_arena + g.at_b);
+      const int lg = g.log2l;
+      const int64_t l = (int64_t)1 << lg;
+      dim3 gp((unsigned)((l + 255) / 256), (unsigned)g.slots);
+      k_fft_pack<<<gp, 256, 0, s>>>((const FftSlot*)(dtab + at_slots[gi]), A, lg);
+      ++launches;
+      float2* z = passes(A, B, lg, g.slots);
+      float2* w = z == A ? B : A;
+      dim3 gq((unsigned)((l + 255) / 256), (unsigned)g.pairs);
+      k_fft_product<<<gq, 256, 0, s>>>(z, (const FftPair*)(dtab + at_pairs[gi]), w, lg);
+      ++launches;
+      float2* v = passes(w, z, lg, g.pairs);
+      if (v != pair_result[gi])
+        return fail(EAR_ERR_STATE, "ear_convolve: internal buffer plan mismatch");
+    }
+    k_fft_accumulate<<<(unsigned)((out_length + 255) / 256), 256, 0, s>>>(
+        (const FftOut*)(dtab + at_outs_placeholder), num, d_out, 0, out_length);
+    ++launches;
+    CU(cudaGetLastError());
+  }
+  CU(cudaEventRecord(sc.ev[1], s));
+  if (!on_dev) CU(cudaMemcpyAsync(out, d_out, sizeof(float) * out_length, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (stats) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]);
+    stats->kernel_ms = ms;
+    stats->launches = launches;
+    stats->fft_points = points;
+    stats->multiply_adds = macs;
+  }
+  return EAR_OK;
+}
+
+}  // extern "C"

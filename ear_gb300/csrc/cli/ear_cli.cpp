@@ -5,18 +5,26 @@
 //   EAR test                            src/EAR.cpp:424-426 (returns 0)
 //   EAR info <file.EAR> [--resave OUT]  parse only: print a summary (no GPU)
 //
+//   EAR wav2raw <in.wav> <out.f32>       WAV -> float samples, as the sources are read
+//   EAR raw2wav <out.wav> <norm> <max> <ch0.f32> [<ch1.f32>]   float -> WAV
+//
 // options: --seed N (default: time(0), as src/EAR.cpp:58), --exact
 // (kernels bit-identical to the CPU restatement), --seconds S (impulse
-// response window, default 8), --device N, --out DIR (where `render` writes
-// the impulse responses when the file sets no debugdir).
+// response window, default 8), --device N, --out DIR (where `render` also
+// writes the impulse responses when the file sets no debugdir), --conv
+// fft|direct (the convolution of the reference built with or without
+// FFTW; default fft), --dump-tracks DIR (also write the post-processed
+// tracks the convolution reads, with their bookkeeping).
 //
 // Render() of the reference (src/EAR.cpp:55-393) is followed step by step:
-// settings, the parse loop, one context per (source x keyframe x band) --
-// here one ear_render call renders all bands of a (source, keyframe) --
-// then Power(0.335), the global maximum, truncation at max/256 and, for
-// `calc T60`, RecorderTrack::T60 with the Sabine and Norris-Eyring
-// predictions.  The convolution with the dry sound (auralisation) is not
-// part of this build: `render` writes the impulse responses instead.
+// settings, the parse loop (the sources' WAVs are read and band-split
+// before rendering), one context per (source x keyframe x band) -- here one
+// ear_render call renders all bands of a (source, keyframe) -- then
+// Power(0.335), the global maximum, truncation at max/256, and either
+// `calc T60` (RecorderTrack::T60 with the Sabine and Norris-Eyring
+// predictions) or the auralisation: every context's section of the dry
+// sound convolved with every recorder track, summed per recorder,
+// normalised and written to the recorder's OUT file.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -24,6 +32,7 @@
 #include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <fstream>
 #include <iomanip>
 #include <iostream>
 #include <map>
@@ -33,12 +42,15 @@
 
 #include "ear_gb300.h"
 #include "earfile.h"
+#include "wavefile.h"
 
 namespace {
 
 struct Options {
   unsigned long long seed = (unsigned long long)time(nullptr);
   bool exact = false;
+  bool conv_direct = false;  // --conv direct: the reference built without FFTW
+  std::string dump;          // --dump-tracks DIR
   double seconds = 8.0;
   int device = 0;
   std::string out;
@@ -59,54 +71,74 @@ earfile::Vec3 at(const std::vector<earfile::Vec3>& v, int kf) {
   return (kf >= 0 && v.size() > 1) ? v[(size_t)kf] : v[0];
 }
 
-// 16-bit PCM WAV, as WaveFile::FromFloat + WaveFile::Save
-// (lib/wave/WaveFile.cpp:124-154, 190-255).
-void write_wav(const std::string& fn, const std::vector<const float*>& ch,
-               const std::vector<int>& len, bool norm, float norm_max) {
-  const int channels = (int)ch.size();
-  int length = 0;
-  for (int l : len) length = std::max(length, l);
-  float max = 1.0f;
-  if (norm) {
-    if (channels == 1) {
-      if (norm_max < 0) {
-        max = -1e9f;
-        for (int i = 0; i < len[0]; ++i) max = std::max(max, std::fabs(ch[0][i]));
-        max /= 0.8f;
-      } else {
-        max = norm_max / 0.95f;
-      }
-    } else {
-      max = -1e9f;
-      for (int c = 0; c < channels; ++c)
-        for (int i = 0; i < len[c]; ++i) max = std::max(max, ch[c][i]);
-      max /= 0.8f;
+// The three band signals of one source: SoundFile::Band (the equalizer
+// split of one WAV) or TripleBandSoundFile::Band (three WAVs), both with
+// offset 0 (src/SoundFile.cpp:149-163).
+struct DryBands {
+  std::vector<float> band[3];
+};
+
+// A sound file name as the reference opens it (relative to the working
+// directory), else relative to the folder of the .EAR file.
+std::string resolve(const std::string& fn, const std::string& ear_path) {
+  if (FILE* f = std::fopen(fn.c_str(), "rb")) {
+    std::fclose(f);
+    return fn;
+  }
+  const size_t slash = ear_path.find_last_of('/');
+  if (slash != std::string::npos && !fn.empty() && fn[0] != '/') {
+    const std::string alt = ear_path.substr(0, slash + 1) + fn;
+    if (FILE* f = std::fopen(alt.c_str(), "rb")) {
+      std::fclose(f);
+      return alt;
     }
   }
-  std::vector<int16_t> pcm((size_t)length * channels, 0);
-  for (int i = 0; i < length; ++i)
-    for (int c = 0; c < channels; ++c)
-      if (i < len[c]) pcm[(size_t)i * channels + c] = (int16_t)(ch[c][i] / max * 32768.0f);
-  FILE* f = std::fopen(fn.c_str(), "wb");
-  if (!f) throw CliError{"cannot write " + fn};
-  const uint32_t data_bytes = (uint32_t)(pcm.size() * 2);
-  const uint32_t riff = data_bytes + 36, fmt_size = 16, rate = 44100;
-  const uint32_t byte_rate = rate * 2 * (uint32_t)channels;
-  const uint16_t format = 1, nch = (uint16_t)channels, align = (uint16_t)(2 * channels), bits = 16;
-  std::fwrite("RIFF", 1, 4, f);
-  std::fwrite(&riff, 4, 1, f);
-  std::fwrite("WAVEfmt ", 1, 8, f);
-  std::fwrite(&fmt_size, 4, 1, f);
-  std::fwrite(&format, 2, 1, f);
-  std::fwrite(&nch, 2, 1, f);
-  std::fwrite(&rate, 4, 1, f);
-  std::fwrite(&byte_rate, 4, 1, f);
-  std::fwrite(&align, 2, 1, f);
-  std::fwrite(&bits, 2, 1, f);
-  std::fwrite("data", 1, 4, f);
-  std::fwrite(&data_bytes, 4, 1, f);
-  std::fwrite(pcm.data(), 2, pcm.size(), f);
-  std::fclose(f);
+  return fn;
+}
+
+// WAV data of every source, split on the GPU (SoundFile::SoundFile and
+// TripleBandSoundFile::TripleBandSoundFile read the WAVs while parsing,
+// src/SoundFile.cpp:33-42, 84-92; a missing file is an error).
+std::vector<DryBands> load_sources(const earfile::Scene& sc, const std::string& ear_path,
+                                   const Options& opt) {
+  const float* fr = sc.freq;  // FREQ block or SoundFile::f1..f3 defaults
+  std::vector<DryBands> out(sc.sources.size());
+  for (size_t s = 0; s < sc.sources.size(); ++s) {
+    const earfile::Source& src = sc.sources[s];
+    if (src.triple) {
+      for (int b = 0; b < 3; ++b) {
+        const std::string fn = b < (int)src.files.size() ? src.files[(size_t)b] : std::string();
+        if (!wav::read_float(resolve(fn, ear_path), &out[s].band[b]))
+          throw CliError{"Failed to open sound file " + fn};
+      }
+    } else {
+      const std::string fn = src.files.empty() ? std::string() : src.files[0];
+      std::vector<float> x;
+      if (!wav::read_float(resolve(fn, ear_path), &x)) throw CliError{"Failed to open sound file " + fn};
+      for (int b = 0; b < 3; ++b) out[s].band[b].resize(x.size());
+      if (ear_band_split(x.data(), (int64_t)x.size(), fr, out[s].band[0].data(),
+                         out[s].band[1].data(), out[s].band[2].data(), 0, nullptr,
+                         opt.device) != EAR_OK)
+        throw CliError{ear_last_error()};
+    }
+  }
+  return out;
+}
+
+// SoundFile::Section(float start, float length) of a band with offset 0
+// (src/SoundFile.cpp:164-173): first sample, sample count, offset.
+void section(size_t sample_length, float start, float length, int64_t* s0, int64_t* n,
+             int64_t* off) {
+  const unsigned int_start = (unsigned)(int)(start * 44100.0f);
+  const unsigned int_length = length < 0 ? (unsigned)sample_length - int_start
+                                          : (unsigned)(int)(length * 44100.0f);
+  if (int_start >= sample_length) {
+    *s0 = *n = *off = 0;
+    return;
+  }
+  *s0 = int_start;
+  *n = std::min<int64_t>(int_length, (int64_t)sample_length - int_start);
+  *off = int_start;
 }
 
 // One rendered (source, keyframe) context: [track][band][bins] + bookkeeping.
@@ -116,6 +148,156 @@ struct Context {
   std::vector<float> hist;
   std::vector<int32_t> first, last;
 };
+
+std::string outdir_debug(const earfile::Scene& sc) {
+  const auto dd = sc.settings.find("debugdir");
+  return dd != sc.settings.end() ? dd->second.s : std::string();
+}
+
+// src/EAR.cpp:292-386: every (source x keyframe x band) context convolves
+// its band section with each recorder's tracks (RecorderContext ->
+// Recorder::Process), keyframe pairs with the next keyframe's response;
+// each recorder then sums its contexts (Recorder::Add), normalises to 0.8
+// (Recorder::Normalize) and saves to its OUT file without further
+// normalisation (Recorder::Save()).  Convolutions run on the GPU.
+void auralise(const earfile::Scene& sc, const std::vector<Context>& contexts, int num_bins, const std::vector<DryBands>& dry, const std::string& debugdir,
+              const Options& opt) {
+  std::cout << std::endl << "Processing data..." << std::endl;
+  const int mode = opt.conv_direct ? EAR_CONV_DIRECT : EAR_CONV_FFT;
+  const int nkeys = (int)sc.keys.size();
+  // the RecorderContext list in its order: (context, band) with the section
+  struct Item {
+    int ctx, band, next;  // next: context of the next keyframe, or -1
+    int64_t s0, n, off;
+  };
+  std::vector<Item> items;
+  for (size_t c = 0; c < contexts.size(); ++c) {
+    const Context& cx = contexts[c];
+    for (int b = 0; b < 3; ++b) {
+      Item it;
+      it.ctx = (int)c;
+      it.band = b;
+      it.next = -1;
+      const size_t len = dry[(size_t)cx.source].band[b].size();
+      if (nkeys) {
+        const float offset = sc.keys[(size_t)cx.keyframe];
+        if (cx.keyframe == nkeys - 1) {
+          section(len, offset, -1.0f, &it.s0, &it.n, &it.off);
+        } else {
+          const float length = sc.keys[(size_t)cx.keyframe + 1] - offset;
+          section(len, offset, length, &it.s0, &it.n, &it.off);
+          it.next = (int)c + 1;  // src/EAR.cpp:311 (*(it+3): the same band one keyframe on)
+        }
+      } else {
+        section(len, 0.0f, -1.0f, &it.s0, &it.n, &it.off);
+      }
+      items.push_back(it);
+    }
+  }
+  auto ctx_of = [&](const Item& it, int t) {
+    const Context& cx = contexts[(size_t)it.ctx];
+    const int i = t * 3 + it.band;
+    ear_conv_context e = {};
+    e.ir = cx.hist.data() + (size_t)i * num_bins;
+    e.ir_capacity = num_bins;
+    e.ir_first = cx.first[(size_t)i];
+    e.ir_length = cx.last[(size_t)i];
+    if (it.next >= 0) {
+      const Context& nx = contexts[(size_t)it.next];
+      e.ir_next = nx.hist.data() + (size_t)i * num_bins;
+      e.ir_next_capacity = num_bins;
+      e.ir_next_first = nx.first[(size_t)i];
+      e.ir_next_length = nx.last[(size_t)i];
+    }
+    const std::vector<float>& band = dry[(size_t)cx.source].band[it.band];
+    e.dry = it.n > 0 ? band.data() + it.s0 : nullptr;
+    e.dry_length = it.n;
+    e.offset = it.off;
+    return e;
+  };
+  double gpu_ms = 0;
+  int64_t conv_calls = 0;
+  // per-context processed recorders (debugdir, src/EAR.cpp:362-372):
+  // Recorder::Save(fn) with the base class defaults, i.e. normalised
+  if (!debugdir.empty()) {
+    int t0 = 0;
+    for (size_t ri = 0; ri < sc.recorders.size(); ++ri) {
+      const int ch = sc.recorders[ri].channels;
+      for (const Item& it : items) {
+        std::vector<std::vector<float>> out((size_t)ch);
+        std::vector<const float*> ptr;
+        std::vector<int> len;
+        for (int k = 0; k < ch; ++k) {
+          ear_conv_context e = ctx_of(it, t0 + k);
+          const int64_t cap = ear_conv_processed_capacity(&e, mode);
+          out[(size_t)k].assign((size_t)cap, 0.0f);
+          ear_conv_stats st = {};
+          if (ear_convolve(&e, 1, mode, out[(size_t)k].data(), cap, 0, nullptr, opt.device, &st) != EAR_OK)
+            throw CliError{ear_last_error()};
+          gpu_ms += st.kernel_ms;
+          ++conv_calls;
+          ptr.push_back(out[(size_t)k].data());
+          len.push_back((int)ear_conv_processed_length(&e, mode));
+        }
+        const Context& cx = contexts[(size_t)it.ctx];
+        std::ostringstream ss;
+        ss << debugdir << "/rec-" << ri << ".sound-" << cx.source;
+        if (cx.keyframe != -1) ss << ".frame-" << std::setw(2) << std::setfill('0') << cx.keyframe;
+        ss << ".band-" << it.band << ".wav";
+        if (!wav::write(ss.str(), ptr, len, true, -1.0f)) throw CliError{"cannot write " + ss.str()};
+      }
+      t0 += ch;
+    }
+  }
+  std::cout << "Merging result..." << std::endl;
+  int t0 = 0;
+  for (size_t ri = 0; ri < sc.recorders.size(); ++ri) {
+    const earfile::Recorder& rec = sc.recorders[ri];
+    const int ch = rec.channels;
+    std::vector<std::vector<float>> out((size_t)ch);
+    std::vector<int> real((size_t)ch);
+    for (int k = 0; k < ch; ++k) {
+      std::vector<ear_conv_context> cs;
+      int64_t cap = 0;
+      for (const Item& it : items) {
+        cs.push_back(ctx_of(it, t0 + k));
+        cap = std::max(cap, ear_conv_processed_capacity(&cs.back(), mode));
+      }
+      out[(size_t)k].assign((size_t)cap, 0.0f);
+      ear_conv_stats st = {};
+      if (ear_convolve(cs.data(), (int32_t)cs.size(), mode, out[(size_t)k].data(), cap, 0, nullptr,
+                       opt.device, &st) != EAR_OK)
+        throw CliError{ear_last_error()};
+      gpu_ms += st.kernel_ms;
+      ++conv_calls;
+      // Recorder::Add reads each processed track over its capacity: the sum
+      // ends at index cap - 1 (its real_length)
+      real[(size_t)k] = (int)(cap - 1);
+    }
+    // Recorder::Normalize(0.8) over the processed tracks
+    // (src/Recorder.cpp:443-460, FloatBuffer::Maximum / Multiply)
+    float max = -1e9f;
+    for (int k = 0; k < ch; ++k) {
+      float x = 0.0f;
+      for (int i = 0; i < real[(size_t)k]; ++i) x = std::max(x, std::fabs(out[(size_t)k][(size_t)i]));
+      max = std::max(max, x);
+    }
+    if (max > 0.0f) {
+      const float f = 0.8f / max;
+      for (int k = 0; k < ch; ++k)
+        for (int i = 0; i < real[(size_t)k]; ++i) out[(size_t)k][(size_t)i] *= f;
+    }
+    std::vector<const float*> ptr;
+    for (int k = 0; k < ch; ++k) ptr.push_back(out[(size_t)k].data());
+    if (!wav::write(rec.filename, ptr, real, false, 1.0f)) throw CliError{"cannot write " + rec.filename};
+    std::cout << " " << rec.filename << ": " << ch << " channel(s), " << *std::max_element(real.begin(), real.end())
+              << " samples" << std::endl;
+    t0 += ch;
+  }
+  std::cout << " convolution (" << (opt.conv_direct ? "direct" : "fft") << "): " << items.size()
+            << " contexts, " << conv_calls << " calls, " << std::setprecision(1) << gpu_ms
+            << " ms on the GPU" << std::setprecision(3) << std::endl;
+}
 
 int render_file(const std::string& path, const Options& opt, bool calc_t60, float* t60) {
   earfile::Scene sc;
@@ -198,6 +380,30 @@ int render_file(const std::string& path, const Options& opt, bool calc_t60, floa
     verts.insert(verts.end(), m.tris.begin(), m.tris.end());
     ids.insert(ids.end(), m.tris.size() / 9, it->second);
     blocks.push_back((int64_t)(m.tris.size() / 9));
+  }
+  const auto dd0 = sc.settings.find("debugdir");
+  const bool has_debugdir = dd0 != sc.settings.end();
+  const bool noprocess0 = sc.settings.count("noprocessing") && sc.settings.at("noprocessing").i > 0;
+  const bool process = !noprocess0 && !calc_t60;
+  std::vector<DryBands> dry;
+  if (process || has_debugdir) dry = load_sources(sc, path, opt);
+  if (has_debugdir && !dry.empty()) {
+    // equalizer output (src/EAR.cpp:122-146): WaveFile::FromFloat without
+    // normalisation; calc T60 keeps the mid band of the first source
+    const std::string dir = dd0->second.s;
+    ::mkdir(dir.c_str(), 0755);
+    const char* lomihi[] = {"low", "mid", "high"};
+    for (size_t s = 0; s < dry.size(); ++s) {
+      for (int b = 0; b < 3; ++b) {
+        if (calc_t60 && b != 1) continue;
+        const std::vector<float>& x = dry[s].band[b];
+        std::ostringstream ss;
+        ss << dir << "/sound-" << s << ".band-" << b << lomihi[b] << ".wav";
+        if (!wav::write(ss.str(), {x.data()}, {(int)x.size()}, false, 1.0f))
+          throw CliError{"cannot write " + ss.str()};
+      }
+      if (calc_t60) break;
+    }
   }
   ear_scene_desc desc = {(int64_t)ids.size(), verts.data(), ids.data(), (int32_t)mats.size(),
                          mats.data(), opt.device};
@@ -303,10 +509,26 @@ int render_file(const std::string& path, const Options& opt, bool calc_t60, floa
       }
     }
 
+  if (!opt.dump.empty()) {
+    // every post-processed track with its bookkeeping, as the convolution
+    // reads them: context-<source>-<keyframe>.f32 = float[tracks][3][bins],
+    // .txt = "tracks bins" then first and last per (track, band)
+    ::mkdir(opt.dump.c_str(), 0755);
+    for (const Context& c : contexts) {
+      std::ostringstream ss;
+      ss << opt.dump << "/context-" << c.source << "-" << c.keyframe;
+      FILE* f = std::fopen((ss.str() + ".f32").c_str(), "wb");
+      if (!f) throw CliError{"cannot write " + ss.str() + ".f32"};
+      std::fwrite(c.hist.data(), sizeof(float), c.hist.size(), f);
+      std::fclose(f);
+      std::ofstream t(ss.str() + ".txt");
+      t << tracks << " " << num_bins << "\n";
+      for (size_t i = 0; i < c.first.size(); ++i) t << c.first[i] << " " << c.last[i] << "\n";
+    }
+  }
   const auto dd = sc.settings.find("debugdir");
   std::string outdir = dd != sc.settings.end() ? dd->second.s : opt.out;
   const bool noprocess = sc.settings.count("noprocessing") && sc.settings.at("noprocessing").i > 0;
-  if (!calc_t60 && outdir.empty()) outdir = path + ".responses";
   if (!outdir.empty()) {
     ::mkdir(outdir.c_str(), 0755);
     const char* lomihi[] = {"low", "mid", "high"};
@@ -327,7 +549,7 @@ int render_file(const std::string& path, const Options& opt, bool calc_t60, floa
             ch.push_back(c.hist.data() + (size_t)i * num_bins);
             len.push_back(std::min(c.last[(size_t)i], num_bins));
           }
-          write_wav(ss.str() + ".wav", ch, len, true, max);
+          if (!wav::write(ss.str() + ".wav", ch, len, true, max)) throw CliError{"cannot write " + ss.str() + ".wav"};
           // FloatBuffer::Write: real_length + 1 floats of track 0 (src/Recorder.cpp:120-123)
           FILE* f = std::fopen((ss.str() + ".bin").c_str(), "wb");
           if (f) {
@@ -341,10 +563,7 @@ int render_file(const std::string& path, const Options& opt, bool calc_t60, floa
   if (noprocess || calc_t60) {
     std::cout << std::endl << "Not processing data" << std::endl;
   } else {
-    std::cout << std::endl
-              << "Auralisation (convolution with the dry sound) is not part of this build; "
-                 "impulse responses written to "
-              << outdir << std::endl;
+    auralise(sc, contexts, num_bins, dry, outdir_debug(sc), opt);
   }
   int rc = 0;
   if (calc_t60) {
@@ -408,6 +627,12 @@ int main(int argc, char** argv) {
     try {
       if (a == "--seed") opt.seed = std::stoull(value("--seed"));
       else if (a == "--exact") opt.exact = true;
+      else if (a == "--dump-tracks") opt.dump = value("--dump-tracks");
+      else if (a == "--conv") {
+        const std::string m = value("--conv");
+        if (m != "fft" && m != "direct") throw CliError{"--conv takes fft or direct"};
+        opt.conv_direct = m == "direct";
+      }
       else if (a == "--seconds") opt.seconds = std::stod(value("--seconds"));
       else if (a == "--device") opt.device = std::stoi(value("--device"));
       else if (a == "--out") opt.out = value("--out");
@@ -452,10 +677,41 @@ int main(int argc, char** argv) {
       return 0;
     } else if (cmd == "info" && !arg1.empty()) {
       return info_file(arg1, resave);
+    } else if (cmd == "wav2raw" && !arg2.empty()) {
+      std::vector<float> x;
+      if (!wav::read_float(arg1, &x)) {
+        std::cout << "Failed to open sound file " << arg1 << std::endl;
+        return 1;
+      }
+      FILE* f = std::fopen(arg2.c_str(), "wb");
+      if (!f) return 1;
+      std::fwrite(x.data(), sizeof(float), x.size(), f);
+      std::fclose(f);
+      std::cout << x.size() << " samples" << std::endl;
+      return 0;
+    } else if (cmd == "raw2wav" && i + 4 < pos.size()) {
+      std::vector<std::vector<float>> chans;
+      for (size_t k = i + 4; k < pos.size() && k < i + 6; ++k) {
+        std::vector<float> x;
+        FILE* f = std::fopen(pos[k].c_str(), "rb");
+        if (!f) return 1;
+        float v;
+        while (std::fread(&v, sizeof v, 1, f) == 1) x.push_back(v);
+        std::fclose(f);
+        chans.push_back(std::move(x));
+      }
+      std::vector<const float*> ptr;
+      std::vector<int> len;
+      for (const auto& c : chans) {
+        ptr.push_back(c.data());
+        len.push_back((int)c.size());
+      }
+      return wav::write(arg1, ptr, len, std::stoi(arg2) != 0, std::stof(pos[i + 3])) ? 0 : 1;
     }
   }
   std::cout << "Usage:" << std::endl
-            << " EAR render <filename> [--seed N] [--exact] [--seconds S] [--out DIR]" << std::endl
+            << " EAR render <filename> [--seed N] [--exact] [--seconds S] [--out DIR]"
+               " [--conv fft|direct]" << std::endl
             << " EAR calc T60 <filename> [--seed N] [--exact] [--seconds S]" << std::endl;
   return 1;
 }

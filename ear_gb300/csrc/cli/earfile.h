@@ -71,7 +71,7 @@ struct Scene {
   bool has_settings = false;
   std::vector<float> keys;  // KEYS
   bool has_freq = false;
-  float freq[3] = {0.2f, 1.0f, 5.0f};
+  float freq[3] = {0.2f, 1.0f, 2.0f};  // SoundFile::f1..f3 defaults (src/SoundFile.cpp:238-240)
   std::vector<Material> materials;
   std::vector<Mesh> meshes;
   std::vector<Recorder> recorders;

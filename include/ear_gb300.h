@@ -432,6 +432,93 @@ ear_status ear_statistical_t60(const float* vertices,
                                const ear_material* first_block_material,
                                float air_absorption_mid, float* out);
 
+/* ------------------------------------------------------------ auralisation
+ * The steps of Render() after the impulse responses (src/EAR.cpp:295-386):
+ * the band split of each dry sound (SoundFile::Band, src/SoundFile.cpp:
+ * 149-160) and the convolution of every recorder track with the dry bands
+ * (RecorderContext -> Recorder::Process -> RecorderTrack::Process, then
+ * Recorder::Add; src/SceneContext.h:59-73, src/Recorder.cpp:136-292,
+ * 343-363, 432-441).  Both run on the GPU.  Pointers are host memory unless
+ * EAR_AURAL_DEVICE_MEMORY is set in `flags`; then every pointer is device
+ * memory and the work is issued on `stream` (the call still returns after it
+ * is complete). */
+#define EAR_AURAL_DEVICE_MEMORY 1u
+
+/* Equalizer::Split (lib/equalizer/Equalizer.cpp:81-96) as SoundFile::Band
+   calls it: 4th-order Linkwitz-Riley low/high passes at the crossovers
+   (f1+f2)/2 and (f2+f3)/2, with f = freq_khz * 1000 (the FREQ block; the
+   reference's defaults are 0.2, 1.0 and 2.0 kHz, src/SoundFile.cpp:238-240).
+   low = LP(x), high = HP(x), mid = HP(LP(x)) at the two crossovers.  The
+   results are bit-identical to the reference's sequential filters. */
+ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3],
+                          float* low, float* mid, float* high, uint32_t flags,
+                          void* stream, int32_t device);
+
+/* Convolution modes of RecorderTrack::Process. */
+#define EAR_CONV_FFT 0    /* builds with FFTW (src/Recorder.cpp:145-243): the
+                             zero-padded product of transforms; a keyframe pair
+                             fades the dry section out under this keyframe's
+                             response and in under the next one's */
+#define EAR_CONV_DIRECT 1 /* builds without FFTW (src/Recorder.cpp:247-292):
+                             the O(N*M) sum, bit-identical to the reference's
+                             loop order; a keyframe pair interpolates the two
+                             responses linearly over the section */
+
+/* One RecorderContext applied to one recorder track: the response `ir`
+   convolved with a section of one band of a dry sound.  The track fields are
+   the FloatBuffer bookkeeping after Power(0.335) and the truncation at
+   max/256 (src/EAR.cpp:209-228): samples [first, length) are the response
+   (the direct mode reads [first, length), the FFT mode [0, length)).
+   `capacity` samples are readable at ir; reads beyond it are 0, as the const
+   FloatBuffer::operator[] (src/Recorder.cpp:61-66). */
+typedef struct ear_conv_context {
+  const float* ir;
+  int64_t ir_capacity;
+  int64_t ir_first;
+  int64_t ir_length;
+  /* next keyframe's response of the same track and band, or NULL
+     (Recorder::Process(sf, r, offset, length), src/Recorder.cpp:352-363) */
+  const float* ir_next;
+  int64_t ir_next_capacity;
+  int64_t ir_next_first;
+  int64_t ir_next_length;
+  const float* dry;   /* the section: SoundFile::Section, src/SoundFile.cpp:164-173 */
+  int64_t dry_length; /* its sample_length (0: an empty section) */
+  int64_t offset;     /* its SoundFile::offset: output index of dry sample 0 */
+} ear_conv_context;
+
+typedef struct ear_conv_stats {
+  float kernel_ms;        /* device time of the convolution kernels */
+  int32_t launches;       /* kernels launched */
+  int64_t fft_points;     /* FFT mode: sum of the transform sizes */
+  double multiply_adds;   /* direct mode: terms summed (incl. padding) */
+} ear_conv_stats;
+
+/* out[x] += sum over contexts c (in order) of processed_c[x - ...] for x in
+   [0, out_length): each context's RecorderTrack::Process result is formed
+   on its own and then added, as Recorder::Add sums the processed tracks of
+   the (source x keyframe x band) contexts of one recorder
+   (src/EAR.cpp:359-377).  In EAR_CONV_DIRECT mode the sums are
+   bit-identical to the reference; in EAR_CONV_FFT mode they agree to FP32
+   transform accuracy.  stats may be NULL. */
+ear_status ear_convolve(const ear_conv_context* contexts, int32_t num_contexts,
+                        int32_t mode, float* out, int64_t out_length,
+                        uint32_t flags, void* stream, int32_t device,
+                        ear_conv_stats* stats);
+
+/* The FloatBuffer capacity (src/Recorder.cpp:33-59, INITIAL 3 s, growth by
+   1 s: src/Recorder.h:36-37) of the track RecorderTrack::Process returns for
+   one context in `mode`.  Recorder::Add reads that many samples, so the
+   processed recorder track ends at max over its contexts of this value,
+   minus one (the WAV length of RecorderTrack::Save). */
+int64_t ear_conv_processed_capacity(const ear_conv_context* context, int32_t mode);
+
+/* The FloatBuffer real_length of that track: the highest index
+   RecorderTrack::Process wrote (0 when it wrote none).  A context's own
+   processed recorder (the debugdir dumps of src/EAR.cpp:362-372) saves this
+   many samples. */
+int64_t ear_conv_processed_length(const ear_conv_context* context, int32_t mode);
+
 #ifdef __cplusplus
 }
 #endif

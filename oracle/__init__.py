@@ -62,6 +62,16 @@ def lib():
         L.oracle_track_length.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float]
         L.oracle_track_t60.restype = C.c_float
         L.oracle_track_t60.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.oracle_band_split.argtypes = [C.c_void_p, C.c_int64, C.c_float, C.c_float, C.c_float,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_process_direct.restype = C.c_int64
+        L.oracle_process_direct.argtypes = ([C.c_void_p] + [C.c_int64] * 3 + [C.c_void_p]
+                                            + [C.c_int64] * 3 + [C.c_void_p, C.c_int64, C.c_int64,
+                                                                 C.c_void_p, C.c_int64])
+        L.oracle_process_fft64.restype = C.c_int64
+        L.oracle_process_fft64.argtypes = ([C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                                            C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
+                                            C.c_int64, C.c_void_p, C.c_int64])
         _L = L
     return _L
 
@@ -171,3 +181,75 @@ def segment_blocked(vertices, origins, dirs):
     out = np.empty(len(o), np.uint8)
     lib().oracle_segment_blocked(C.byref(d), len(o), o.ctypes.data, r.ctypes.data, out.ctypes.data)
     return out.astype(bool)
+
+
+# ------------------------------------------------------------ auralisation
+# Restatements of Equalizer::Split and RecorderTrack::Process; contexts are
+# ear_gb300.aural.Context objects with numpy buffers.
+
+def band_split(dry, freq_khz=(0.2, 1.0, 2.0)):
+    x = np.ascontiguousarray(dry, np.float32)
+    outs = [np.empty_like(x) for _ in range(3)]
+    lib().oracle_band_split(x.ctypes.data, x.size, *[float(f) for f in freq_khz],
+                            *[o.ctypes.data for o in outs])
+    return tuple(outs)
+
+
+def _track(t):
+    a = np.ascontiguousarray(t.data, np.float32)
+    return a, (a.ctypes.data if a.size else None), a.size
+
+
+def process_direct(ctx, out_length):
+    """RecorderTrack::Process without FFTW for one context: (track of
+    out_length samples, FloatBuffer capacity)."""
+    a, pa, ca = _track(ctx.ir)
+    d = np.ascontiguousarray(ctx.dry, np.float32)
+    out = np.zeros(int(out_length), np.float32)
+    if ctx.ir_next is not None:
+        b, pb, cb = _track(ctx.ir_next)
+        nf, nl = ctx.ir_next.first, ctx.ir_next.length
+    else:
+        b, pb, cb, nf, nl = None, None, 0, 0, 0
+    cap = lib().oracle_process_direct(pa, ca, ctx.ir.first, ctx.ir.length, pb, cb, nf, nl,
+                                      d.ctypes.data if d.size else None, d.size, ctx.offset,
+                                      out.ctypes.data, out.size)
+    return out, int(cap)
+
+
+def process_fft64(ctx, out_length):
+    """The FFTW-build RecorderTrack::Process for one context in float64:
+    (values of out_length samples, FloatBuffer capacity)."""
+    a, pa, ca = _track(ctx.ir)
+    d = np.ascontiguousarray(ctx.dry, np.float32)
+    out = np.zeros(int(out_length), np.float64)
+    if ctx.ir_next is not None:
+        b, pb, cb = _track(ctx.ir_next)
+        nl = ctx.ir_next.length
+    else:
+        b, pb, cb, nl = None, None, 0, 0
+    cap = lib().oracle_process_fft64(pa, ca, ctx.ir.length, pb, cb, nl,
+                                     d.ctypes.data if d.size else None, d.size, ctx.offset,
+                                     out.ctypes.data, out.size)
+    return out, int(cap)
+
+
+def convolve_direct(contexts, out_length):
+    """Recorder::Add of the processed tracks, in float32 and in order."""
+    total = np.zeros(int(out_length), np.float32)
+    caps = []
+    for c in contexts:
+        t, cap = process_direct(c, out_length)
+        total = total + t
+        caps.append(cap)
+    return total, caps
+
+
+def convolve_fft64(contexts, out_length):
+    total = np.zeros(int(out_length), np.float64)
+    caps = []
+    for c in contexts:
+        t, cap = process_fft64(c, out_length)
+        total += t
+        caps.append(cap)
+    return total, caps

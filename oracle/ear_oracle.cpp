@@ -1024,4 +1024,169 @@ float oracle_track_t60(const float* data, int32_t first, int32_t last) {
   return (float)(last_significant_offset - direct_sound_offset) / 44100.0f;
 }
 
+
+// ----------------------------------------------------------- auralisation
+// Equalizer (lib/equalizer/Equalizer.cpp:26-96): 4th-order Linkwitz-Riley
+// passes, restated with the same constants and operation order.
+struct OLr {
+  float b1, b2, b3, b4, a0, a1, a2, a3, a4;
+  float xm1 = 0, xm2 = 0, xm3 = 0, xm4 = 0, ym1 = 0, ym2 = 0, ym3 = 0, ym4 = 0;
+  OLr(float fc, bool high) {
+    const float srate = 44100.0f;
+    const float pi = 3.14285714285714f;
+    float wc = 2.0f * pi * srate;
+    float wc2 = wc * wc;
+    float wc3 = wc2 * wc;
+    float wc4 = wc2 * wc2;
+    float k = wc / std::tan(pi * fc / srate);
+    float k2 = k * k;
+    float k3 = k2 * k;
+    float k4 = k2 * k2;
+    float sqrt2 = std::sqrt(2.0f);
+    float sq_tmp1 = sqrt2 * wc3 * k;
+    float sq_tmp2 = sqrt2 * wc * k3;
+    float a_tmp = 4.0f * wc2 * k2 + 2.0f * sq_tmp1 + k4 + 2.0f * sq_tmp2 + wc4;
+    b1 = (4.0f * (wc4 + sq_tmp1 - k4 - sq_tmp2)) / a_tmp;
+    b2 = (6.0f * wc4 - 8.0f * wc2 * k2 + 6.0f * k4) / a_tmp;
+    b3 = (4.0f * (wc4 - sq_tmp1 + sq_tmp2 - k4)) / a_tmp;
+    b4 = (k4 - 2.0f * sq_tmp1 + wc4 - 2.0f * sq_tmp2 + 4.0f * wc2 * k2) / a_tmp;
+    const float g = high ? k4 : wc4;
+    a0 = g / a_tmp;
+    a1 = (high ? -4.0f : 4.0f) * g / a_tmp;
+    a2 = 6.0f * g / a_tmp;
+    a3 = a1;
+    a4 = a0;
+  }
+  float step(float in) {
+    const float out = a0 * in + a1 * xm1 + a2 * xm2 + a3 * xm3 + a4 * xm4 - b1 * ym1 - b2 * ym2 -
+                      b3 * ym3 - b4 * ym4;
+    xm4 = xm3; xm3 = xm2; xm2 = xm1; xm1 = in;
+    ym4 = ym3; ym3 = ym2; ym2 = ym1; ym1 = out;
+    return out;
+  }
+};
+
+// FloatBuffer with the reference's growth and bookkeeping
+// (src/Recorder.cpp:33-66): writes through at(), reads through get().
+struct OBuf {
+  std::vector<float> data;
+  int64_t real_length = 0, first_sample = 3 * 44100 - 1;
+  OBuf() : data((size_t)(3 * 44100), 0.0f) {}
+  int64_t length() const { return (int64_t)data.size(); }
+  float& at(int64_t i) {
+    if (i >= length()) data.resize((size_t)(i + 44100), 0.0f);
+    if (i > real_length) real_length = i;
+    if (i < first_sample) first_sample = i;
+    return data[(size_t)i];
+  }
+  float get(int64_t i) const { return i < length() ? data[(size_t)i] : 0.0f; }
+};
+
+int64_t copy_out(const OBuf& b, float* out, int64_t out_cap) {
+  const int64_t n = std::min(out_cap, b.length());
+  std::memcpy(out, b.data.data(), sizeof(float) * (size_t)n);
+  for (int64_t i = n; i < out_cap; ++i) out[i] = 0.0f;
+  return b.length();
+}
+
+// A response track as the caller passes it: `cap` samples at p, zero
+// beyond (the const FloatBuffer::operator[]).
+struct OResp {
+  const float* p;
+  int64_t cap;
+  float get(int64_t j) const { return j < cap ? p[j] : 0.0f; }
+};
+
+// Equalizer::Split (lib/equalizer/Equalizer.cpp:81-96) as SoundFile::Band
+// calls it (frequencies in kHz times 1000, src/SoundFile.cpp:153).
+void oracle_band_split(const float* data, int64_t n, float f1k, float f2k, float f3k, float* low,
+                       float* mid, float* high) {
+  const float f1 = f1k * 1000.0f, f2 = f2k * 1000.0f, f3 = f3k * 1000.0f;
+  const float fc1 = (f1 + f2) / 2.0f;
+  const float fc2 = (f2 + f3) / 2.0f;
+  OLr hi_pass1(fc1, true), hi_pass2(fc2, true), lo_pass1(fc1, false), lo_pass2(fc2, false);
+  for (int64_t i = 0; i < n; ++i) {
+    high[i] = hi_pass2.step(data[i]);
+    low[i] = lo_pass1.step(data[i]);
+    mid[i] = lo_pass2.step(data[i]);
+    mid[i] = hi_pass1.step(mid[i]);
+  }
+}
+
+// RecorderTrack::Process of builds without FFTW (src/Recorder.cpp:247-292),
+// loop for loop: the plain variant over [first, len) of the track, the
+// keyframe variant (ir2 != NULL) over [min first, max len) of both with the
+// linear interpolation.  Writes the processed track (zero-padded to
+// out_cap) and returns its FloatBuffer capacity.
+int64_t oracle_process_direct(const float* ir, int64_t cap, int64_t first, int64_t len,
+                              const float* ir2, int64_t cap2, int64_t first2, int64_t len2,
+                              const float* dry, int64_t n, int64_t offset, float* out,
+                              int64_t out_cap) {
+  OBuf result;
+  const OResp a{ir, cap}, b{ir2, cap2};
+  if (!ir2) {
+    for (int64_t i = 0; i < n; ++i) {
+      const float sfs = dry[i];
+      int64_t index = i + offset + first;
+      for (int64_t j = first; j < len; ++j) result.at(index++) += sfs * a.get(j);
+    }
+  } else {
+    const float flt_samples = 1.0f / (float)(uint32_t)n;
+    const int64_t l = std::max(len, len2);
+    const int64_t f = std::min(first, first2);
+    for (int64_t i = 0; i < n; ++i) {
+      const float i1 = (float)(uint32_t)i * flt_samples;
+      const float i2 = 1.0f - i1;
+      const float sfs = dry[i];
+      int64_t index = i + offset + f;
+      for (int64_t j = f; j < l; ++j) {
+        const float p = i2 * a.get(j) + i1 * b.get(j);
+        result.at(index++) += sfs * p;
+      }
+    }
+  }
+  return copy_out(result, out, out_cap);
+}
+
+// The FFT variant (src/Recorder.cpp:145-243) in double precision: the
+// response [0, len) convolved with the dry section, faded as the reference
+// fades it (FP32 ramp stepped in sequence, FP32 products), written to
+// offset + [0, len + n + 1).  For a keyframe pair the faded-out and faded-in
+// results are summed (RecorderTrack::Add).  out64 receives the values,
+// zero-padded to out_cap; the return value is the capacity of the processed
+// track.
+int64_t oracle_process_fft64(const float* ir, int64_t cap, int64_t len, const float* ir2,
+                             int64_t cap2, int64_t len2, const float* dry, int64_t n,
+                             int64_t offset, double* out64, int64_t out_cap) {
+  for (int64_t i = 0; i < out_cap; ++i) out64[i] = 0.0;
+  auto one = [&](const OResp& t, int64_t m, int fade, OBuf* shape) {
+    std::vector<float> b((size_t)n);
+    for (int64_t i = 0; i < n; ++i) b[(size_t)i] = dry[i];
+    if (fade != 0) {
+      float factor = fade < 0 ? 1.0f : 0.0f;
+      const float df = (fade < 0 ? -1.0f : 1.0f) / (float)(uint32_t)n;
+      for (int64_t i = 0; i < n; ++i) {
+        b[(size_t)i] *= factor;
+        factor += df;
+      }
+    }
+    const int64_t mn = m + n + 1;
+    for (int64_t x = 0; x < mn; ++x) {
+      double acc = 0.0;
+      const int64_t lo = std::max<int64_t>(0, x - (m - 1)), hi = std::min<int64_t>(n - 1, x);
+      for (int64_t i = lo; i <= hi; ++i) acc += (double)b[(size_t)i] * (double)t.get(x - i);
+      if (offset + x < out_cap) out64[offset + x] += acc;
+      shape->at(offset + x) += 0.0f;  // the reference writes every index
+    }
+  };
+  OBuf ra;
+  one(OResp{ir, cap}, len, ir2 ? -1 : 0, &ra);
+  if (!ir2) return ra.length();
+  OBuf rb;
+  one(OResp{ir2, cap2}, len2, 1, &rb);
+  const int64_t lb = rb.length();  // RecorderTrack::Add reads getLength(0.0f)
+  for (int64_t i = 0; i < lb; ++i) ra.at(i) += rb.get(i);
+  return ra.length();
+}
+
 }  // extern "C"

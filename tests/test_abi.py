@@ -44,7 +44,8 @@ def test_ctypes_layout_matches_c():
         "ear_render_params": N.EarRenderParams, "ear_render_stats": N.EarRenderStats,
         "ear_histograms": N.EarHistograms, "ear_batch_job": N.EarBatchJob,
         "ear_batch_config": N.EarBatchConfig, "ear_tune_opts": N.EarTuneOpts,
-        "ear_tune_result": N.EarTuneResult,
+        "ear_tune_result": N.EarTuneResult, "ear_conv_context": N.EarConvContext,
+        "ear_conv_stats": N.EarConvStats,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ear_gb300.h"', "int main(){"]
     for cname, py in structs.items():
