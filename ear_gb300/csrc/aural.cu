@@ -4,14 +4,14 @@
 //
 //  * Band split (Equalizer::Split, lib/equalizer/Equalizer.cpp:81-96): four
 //    IIR recurrences per signal.  Each output sample depends on the previous
-//    four, in FP32, so the filters run sequentially -- one thread per output
-//    chain (low, high, and mid = HP(LP(x))) -- with the reference's operation
+//    four, in FP32, so each filter runs sequentially -- one lane per filter
+//    (low, high, and mid = HP(LP(x))) -- with the reference's operation
 //    order (explicit _rn intrinsics, no contraction): bit-identical outputs.
 //  * Direct convolution (RecorderTrack::Process without FFTW,
 //    src/Recorder.cpp:247-292): out[x] = sum_i s_i * h(x - off - i), summed
 //    for each x in ascending i as the reference's loop nest does, then added
 //    to the recorder total context by context.  Register-blocked: a thread
-//    owns kDirR consecutive outputs and slides the response window through
+//    owns R consecutive outputs and slides the response window through
 //    registers; dry and response chunks are staged in shared memory.  The
 //    sum order is the reference's, so the results are bit-identical.
 //  * FFT convolution (the FFTW build, src/Recorder.cpp:145-243): a
@@ -80,64 +80,92 @@ LrFilter lr_filter(float fc, bool high) {
   return f;
 }
 
-struct LrState {
-  float x1, x2, x3, x4, y1, y2, y3, y4;
-};
-
-// Equalizer::Pass::Process (lib/equalizer/Equalizer.cpp:26-31), evaluated
-// left to right as written.
-__device__ __forceinline__ float lr_step(const LrFilter& f, LrState& s, float in) {
-  float o = __fmul_rn(f.a0, in);
-  o = __fadd_rn(o, __fmul_rn(f.a1, s.x1));
-  o = __fadd_rn(o, __fmul_rn(f.a2, s.x2));
-  o = __fadd_rn(o, __fmul_rn(f.a3, s.x3));
-  o = __fadd_rn(o, __fmul_rn(f.a4, s.x4));
-  o = __fsub_rn(o, __fmul_rn(f.b1, s.y1));
-  o = __fsub_rn(o, __fmul_rn(f.b2, s.y2));
-  o = __fsub_rn(o, __fmul_rn(f.b3, s.y3));
-  o = __fsub_rn(o, __fmul_rn(f.b4, s.y4));
-  s.x4 = s.x3;
-  s.x3 = s.x2;
-  s.x2 = s.x1;
-  s.x1 = in;
-  s.y4 = s.y3;
-  s.y3 = s.y2;
-  s.y2 = s.y1;
-  s.y1 = o;
-  return o;
-}
-
 struct SplitArgs {
   const float* x;
   float* out[3];  // low, mid, high
   int64_t n;
-  LrFilter lp1, lp2, hp1, hp2;  // crossovers 1 and 2
+  LrFilter f[4];  // per lane: LP1, HP2, LP2, HP1 (crossovers 1 and 2)
 };
 
-constexpr int kSplitBatch = 16;
+constexpr int kSplitBlock = 16;
 
-// Thread 0: low = LP1(x); thread 1: high = HP2(x); thread 2: mid =
-// HP1(LP2(x)).  Inputs are read in batches so the loads overlap the
-// recurrence.
-__global__ void k_band_split(SplitArgs a) {
-  const int c = threadIdx.x;
-  if (c > 2) return;
-  const LrFilter f0 = c == 0 ? a.lp1 : (c == 1 ? a.hp2 : a.lp2);
-  const LrFilter& f1 = a.hp1;
-  LrState s0 = {0, 0, 0, 0, 0, 0, 0, 0}, s1 = s0;
-  float* out = a.out[c == 0 ? 0 : (c == 1 ? 2 : 1)];
-  float buf[kSplitBatch];
-  for (int64_t t0 = 0; t0 < a.n; t0 += kSplitBatch) {
-    const int m = (int)(a.n - t0 < kSplitBatch ? a.n - t0 : kSplitBatch);
+// One warp; lanes 0-3 run one filter each: lane 0 low = LP1(x), lane 1
+// high = HP2(x), lane 2 LP2(x), lane 3 mid = HP1(LP2(x)).  The lanes
+// advance in lock step through blocks of kSplitBlock samples; lane 3
+// filters the block lane 2 finished one block earlier (handed over with
+// shuffles between blocks).
+//
+// Equalizer::Pass::Process (lib/equalizer/Equalizer.cpp:26-31) evaluates
+//   out = a0*in + a1*xm1 + a2*xm2 + a3*xm3 + a4*xm4 - b1*ym1 - b2*ym2
+//         - b3*ym3 - b4*ym4
+// left to right.  Its first five terms involve only inputs, so for a whole
+// block they are formed first, as independent chains; the recurrence then
+// only subtracts the four feedback products in the same order.  Every
+// operation and its rounding are the reference's, so the outputs are the
+// sequential filters' bits; the serial chain per sample shrinks to one
+// multiply and four subtractions.
+__global__ void __launch_bounds__(32) k_band_split(SplitArgs a) {
+  constexpr int B = kSplitBlock;
+  const int lane = threadIdx.x;
+  const LrFilter f = a.f[lane & 3];
+  float* out = lane == 0 ? a.out[0] : (lane == 1 ? a.out[2] : a.out[1]);
+  const bool writer = lane == 0 || lane == 1 || lane == 3;
+  const int64_t nblk = (a.n + B - 1) / B;
+  float x1 = 0.0f, x2 = 0.0f, x3 = 0.0f, x4 = 0.0f;  // previous inputs
+  float y1 = 0.0f, y2 = 0.0f, y3 = 0.0f, y4 = 0.0f;  // previous outputs
+  float xb[B], lp2[B];
 #pragma unroll
-    for (int u = 0; u < kSplitBatch; ++u) buf[u] = u < m ? __ldg(a.x + t0 + u) : 0.0f;
+  for (int u = 0; u < B; ++u) {
+    xb[u] = u < a.n ? __ldg(a.x + u) : 0.0f;
+    lp2[u] = 0.0f;
+  }
+  for (int64_t k = 0; k <= nblk; ++k) {
+    // lane 3 filters block k - 1 (from lp2); the others block k
+    float in[B];
 #pragma unroll
-    for (int u = 0; u < kSplitBatch; ++u) {
-      if (u < m) {
-        float y = lr_step(f0, s0, buf[u]);
-        if (c == 2) y = lr_step(f1, s1, y);
-        out[t0 + u] = y;
-      }
+    for (int u = 0; u < B; ++u) in[u] = lane == 3 ? lp2[u] : xb[u];
+    const int64_t tn = (k + 1) * B;
+#pragma unroll
+    for (int u = 0; u < B; ++u) xb[u] = tn + u < a.n ? __ldg(a.x + tn + u) : 0.0f;
+    // the input terms, a0*in + a1*xm1 + a2*xm2 + a3*xm3 + a4*xm4
+    float p[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const float m1 = u >= 1 ? in[u - 1] : x1;
+      const float m2 = u >= 2 ? in[u - 2] : (u == 1 ? x1 : x2);
+      const float m3 = u >= 3 ? in[u - 3] : (u == 2 ? x1 : (u == 1 ? x2 : x3));
+      const float m4 = u >= 4 ? in[u - 4] : (u == 3 ? x1 : (u == 2 ? x2 : (u == 1 ? x3 : x4)));
+      float o = __fmul_rn(f.a0, in[u]);
+      o = __fadd_rn(o, __fmul_rn(f.a1, m1));
+      o = __fadd_rn(o, __fmul_rn(f.a2, m2));
+      o = __fadd_rn(o, __fmul_rn(f.a3, m3));
+      p[u] = __fadd_rn(o, __fmul_rn(f.a4, m4));
+    }
+    x4 = in[B - 4];
+    x3 = in[B - 3];
+    x2 = in[B - 2];
+    x1 = in[B - 1];
+    // the feedback terms, - b1*ym1 - b2*ym2 - b3*ym3 - b4*ym4
+    float ob[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      float o = __fsub_rn(p[u], __fmul_rn(f.b1, y1));
+      o = __fsub_rn(o, __fmul_rn(f.b2, y2));
+      o = __fsub_rn(o, __fmul_rn(f.b3, y3));
+      o = __fsub_rn(o, __fmul_rn(f.b4, y4));
+      y4 = y3;
+      y3 = y2;
+      y2 = y1;
+      y1 = o;
+      ob[u] = o;
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) lp2[u] = __shfl_sync(0xffffffffu, ob[u], 2);
+    const int64_t t0 = lane == 3 ? (k - 1) * B : k * B;
+    if (writer && t0 >= 0) {
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (t0 + u < a.n) out[t0 + u] = ob[u];
     }
   }
 }
@@ -160,10 +188,16 @@ struct DirectCtx {
 };
 
 constexpr int kDirThreads = 128;
-constexpr int kDirR = 9;  // outputs per thread; odd, so the window loads are bank-conflict free
-constexpr int kDirTile = kDirThreads * kDirR;
-constexpr int kDirChunk = 28 * kDirR;  // dry samples staged per step
-constexpr int kDirWin = kDirTile + kDirChunk - 1;
+// Outputs per thread: odd, so the window loads are bank-conflict free (9
+// measured fastest: 13 cost a third more time through fewer resident
+// blocks and spills).
+template <bool ANY_INTERP>
+struct DirShape {
+  static constexpr int R = 9;
+  static constexpr int Tile = kDirThreads * R;
+  static constexpr int Chunk = 28 * R;  // dry samples staged per step
+  static constexpr int Win = Tile + Chunk - 1;
+};
 
 __device__ __forceinline__ float dir_h(const float* p, int64_t cap, int64_t j, int64_t lo,
                                        int64_t hi) {
@@ -171,9 +205,10 @@ __device__ __forceinline__ float dir_h(const float* p, int64_t cap, int64_t j, i
 }
 
 // Sum of one context over the block's tile into acc (from +0, ascending i).
-template <bool INTERP>
+template <bool INTERP, typename SH>
 __device__ __forceinline__ void direct_context(const DirectCtx& C, int64_t x0, int t, float* s_dry,
-                                               float* s_h, float* s_h2, float (&acc)[kDirR]) {
+                                               float* s_h, float* s_h2, float (&acc)[SH::R]) {
+  constexpr int kDirR = SH::R, kDirTile = SH::Tile, kDirChunk = SH::Chunk, kDirWin = SH::Win;
   // dry indices that reach this tile
   const int64_t ilo = max((int64_t)0, x0 - C.off - C.len + 1);
   const int64_t ihi = min(C.n - 1, x0 + kDirTile - 1 - C.off - C.first);
@@ -245,6 +280,8 @@ template <bool ANY_INTERP>
 __global__ void __launch_bounds__(kDirThreads) k_conv_direct(const DirectCtx* __restrict__ ctxs,
                                                              int num_ctx, float* __restrict__ out,
                                                              int64_t out_len) {
+  using SH = DirShape<ANY_INTERP>;
+  constexpr int kDirR = SH::R, kDirTile = SH::Tile, kDirChunk = SH::Chunk, kDirWin = SH::Win;
   __shared__ float s_dry[kDirChunk];
   __shared__ float s_h[kDirWin];
   __shared__ float s_h2[ANY_INTERP ? kDirWin : 1];
@@ -262,9 +299,9 @@ __global__ void __launch_bounds__(kDirThreads) k_conv_direct(const DirectCtx* __
 #pragma unroll
     for (int r = 0; r < kDirR; ++r) acc[r] = 0.0f;
     if (ANY_INTERP && C.interp)
-      direct_context<true>(C, x0, t, s_dry, s_h, s_h2, acc);
+      direct_context<true, SH>(C, x0, t, s_dry, s_h, s_h2, acc);
     else
-      direct_context<false>(C, x0, t, s_dry, s_h, s_h2, acc);
+      direct_context<false, SH>(C, x0, t, s_dry, s_h, s_h2, acc);
 #pragma unroll
     for (int r = 0; r < kDirR; ++r) total[r] = __fadd_rn(total[r], acc[r]);
   }
@@ -614,10 +651,10 @@ ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3], 
   const float f1 = freq_khz[0] * 1000.0f, f2 = freq_khz[1] * 1000.0f, f3 = freq_khz[2] * 1000.0f;
   const float fc1 = (f1 + f2) / 2.0f, fc2 = (f2 + f3) / 2.0f;
   SplitArgs a;
-  a.lp1 = lr_filter(fc1, false);
-  a.lp2 = lr_filter(fc2, false);
-  a.hp1 = lr_filter(fc1, true);
-  a.hp2 = lr_filter(fc2, true);
+  a.f[0] = lr_filter(fc1, false);  // lo_pass1 -> low
+  a.f[1] = lr_filter(fc2, true);   // hi_pass2 -> high
+  a.f[2] = lr_filter(fc2, false);  // lo_pass2
+  a.f[3] = lr_filter(fc1, true);   // hi_pass1 (of lo_pass2) -> mid
   a.n = n;
   const bool on_dev = flags & EAR_AURAL_DEVICE_MEMORY;
   cudaStream_t s = on_dev ? (cudaStream_t)stream : nullptr;
@@ -801,13 +838,14 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       d.inv_n = c.dry_length > 0 ? 1.0f / (float)(uint32_t)c.dry_length : 0.0f;
       d.interp = c.ir_next ? 1 : 0;
       any_interp |= d.interp != 0;
-      if (d.len > d.first && d.n > 0) macs += (double)d.n * (double)(d.len - d.first + kDirTile);
+      if (d.len > d.first && d.n > 0) macs += (double)d.n * (double)(d.len - d.first);
     }
     const size_t at = push(dc.data(), sizeof(DirectCtx) * num);
     CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
     CU(cudaMemcpyAsync(sc.tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
     const DirectCtx* d_ctx = (const DirectCtx*)(sc.tab + at);
-    const int64_t blocks = (out_length + kDirTile - 1) / kDirTile;
+    const int tile = any_interp ? DirShape<true>::Tile : DirShape<false>::Tile;
+    const int64_t blocks = (out_length + tile - 1) / tile;
     if (blocks > 0x7fffffffLL) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output too long");
     if (any_interp)
       k_conv_direct<true><<<(unsigned)blocks, kDirThreads, 0, s>>>(d_ctx, num, d_out, out_length);

@@ -491,7 +491,7 @@ typedef struct ear_conv_stats {
   float kernel_ms;        /* device time of the convolution kernels */
   int32_t launches;       /* kernels launched */
   int64_t fft_points;     /* FFT mode: sum of the transform sizes */
-  double multiply_adds;   /* direct mode: terms summed (incl. padding) */
+  double multiply_adds;   /* direct mode: terms of the reference's sums, n * (len - first) per context */
 } ear_conv_stats;
 
 /* out[x] += sum over contexts c (in order) of processed_c[x - ...] for x in

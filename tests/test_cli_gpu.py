@@ -89,7 +89,7 @@ def test_render_writes_impulse_responses(tmp_path):
         assert pcm.shape[1] == ch and pcm.shape[0] > 44100
         peak = np.abs(pcm.astype(np.int64)).max()
         assert 0.79 * 32768 <= peak <= 0.8 * 32768 + 1  # Normalize(0.8), Save without norm
-    wavs = sorted(p.name for p in tmp_path.glob("*.wav"))
+    wavs = sorted(p.name for p in tmp_path.glob("response-*.wav"))
     # 2 recorders x 3 bands, reference naming (src/EAR.cpp:234-238)
     assert wavs == sorted(f"response-{i}.sound-0.band-{b}{n}.wav" for i in range(2)
                           for b, n in enumerate(["low", "mid", "high"]))

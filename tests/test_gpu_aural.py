@@ -98,14 +98,12 @@ def test_direct_convolution_adds_to_out_and_clips():
     n_out = 4100  # shorter than the processed tracks: clipped
     base = (rng.standard_normal(n_out) * 1e-3).astype(np.float32)
     got, _ = aural.convolve(ctxs, "direct", out=base.copy())
-    ref, _ = oracle.convolve_direct(ctxs, 200000)
-    # out = base + t1 + t2 + t3 in order; the oracle total starts from 0
+    # out = base + t1 + t2 + t3 in order, each t the context's own sum
     exp = base.copy()
     for c in ctxs:
         t, _ = oracle.process_direct(c, n_out)
         exp = exp + t
     np.testing.assert_array_equal(bits(got), bits(exp))
-    assert np.abs(ref[:n_out] - got).max() < 1e-3
 
 
 @pytest.mark.parametrize("name", CASES)
