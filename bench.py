@@ -22,6 +22,9 @@ roofline   algorithmic bytes of the trace kernel (64 B per node visit, 48 B
            measured HBM copy bandwidth.
 cpu_baseline  the CPU restatement of the reference algorithm (brute-force
            triangle loops, oracle/), all host threads, on a bounded ray sample.
+auralisation  the steps after the impulse responses (band split, FFT and
+           direct convolution of 10 tracks x 3 bands, 4 s x 10 s) with their
+           CPU legs; --aural-only runs this part alone.
 
 Multi-GPU (torchrun): rays are independent, so rank r renders rays
 [r*N, (r+1)*N) of the same random stream (ear_render_params.first_ray) with
