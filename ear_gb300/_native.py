@@ -114,6 +114,7 @@ class EarTuneResult(C.Structure):
 
 
 EAR_AURAL_DEVICE_MEMORY = 1
+EAR_SPLIT_CHUNKED = 2
 EAR_CONV_FFT = 0
 EAR_CONV_DIRECT = 1
 

@@ -170,6 +170,154 @@ __global__ void __launch_bounds__(32) k_band_split(SplitArgs a) {
   }
 }
 
+// ---- chunked band split (EAR_SPLIT_CHUNKED): the same filters evaluated
+// in parallel over chunks of kIirChunk samples.  The recurrence is linear:
+// a chunk's output is its response from a zero feedback state (inputs and
+// their history known) plus the homogeneous response of the true entry
+// state.  Phase 1 runs every chunk from a zero state and keeps its last four
+// outputs end0(c).  The entry states follow entry(c+1) = M^K entry(c) +
+// end0(c) (M: the 4x4 companion matrix of the feedback terms); the filters
+// are stable and K = 512 steps shrink M^K far below rounding (|M^K| ~ 1e-6
+// for a 600 Hz crossover), so phase 2 unrolls that recurrence only `depth`
+// chunks back, entry(c) = sum_{i=1..depth} M^(K(i-1)) end0(c-i) in double,
+// with depth chosen on the host so that |M^K|^depth < 1e-12; each chunk
+// computes its own entry and re-runs from it.  Chunk 0 starts from
+// the true (zero) state, so it is bit-identical to the sequential filter;
+// later chunks start from entry states closer to exact arithmetic than the
+// sequential FP32 run's, so they follow a different rounding path: both stay
+// within the filters' FP32 accuracy (about 1e-3 of the peak in the low
+// band), but not bit for bit.
+constexpr int kIirChunk = 512;
+
+struct IirJob {
+  const float* x;
+  float* y;
+  int64_t n;
+  LrFilter f;
+  double mk[16];  // M^kIirChunk, row-major
+  int depth;      // chunks back that reach an entry state
+};
+
+// One chunk of the filter from the given feedback state (y1..y4); input
+// history read from x.  Inputs are loaded 16 at a time ahead of the
+// recurrence, so the loads overlap it.
+__device__ __forceinline__ void iir_chunk(const IirJob& J, int64_t t0, int64_t t1, float y1,
+                                          float y2, float y3, float y4, float* y_out,
+                                          float* end) {
+  const LrFilter& f = J.f;
+  float x1 = t0 >= 1 ? J.x[t0 - 1] : 0.0f, x2 = t0 >= 2 ? J.x[t0 - 2] : 0.0f;
+  float x3 = t0 >= 3 ? J.x[t0 - 3] : 0.0f, x4 = t0 >= 4 ? J.x[t0 - 4] : 0.0f;
+  for (int64_t tb = t0; tb < t1; tb += 16) {
+    float xin[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) xin[u] = tb + u < t1 ? __ldg(J.x + tb + u) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      if (tb + u >= t1) break;
+      const float in = xin[u];
+      float o = __fmul_rn(f.a0, in);
+      o = __fadd_rn(o, __fmul_rn(f.a1, x1));
+      o = __fadd_rn(o, __fmul_rn(f.a2, x2));
+      o = __fadd_rn(o, __fmul_rn(f.a3, x3));
+      o = __fadd_rn(o, __fmul_rn(f.a4, x4));
+      o = __fsub_rn(o, __fmul_rn(f.b1, y1));
+      o = __fsub_rn(o, __fmul_rn(f.b2, y2));
+      o = __fsub_rn(o, __fmul_rn(f.b3, y3));
+      o = __fsub_rn(o, __fmul_rn(f.b4, y4));
+      x4 = x3;
+      x3 = x2;
+      x2 = x1;
+      x1 = in;
+      y4 = y3;
+      y3 = y2;
+      y2 = y1;
+      y1 = o;
+      if (y_out) y_out[tb + u] = o;
+    }
+  }
+  if (end) {
+    end[0] = y1;
+    end[1] = y2;
+    end[2] = y3;
+    end[3] = y4;
+  }
+}
+
+// Phase 1: blockIdx.y = job, one thread per chunk; end0[job][chunk][4].
+__global__ void k_iir_zero(const IirJob* __restrict__ jobs, float* __restrict__ end0, int chunks) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= chunks) return;
+  const IirJob& J = jobs[blockIdx.y];
+  const int64_t t0 = (int64_t)c * kIirChunk;
+  if (t0 >= J.n) return;
+  const int64_t t1 = min(J.n, t0 + kIirChunk);
+  iir_chunk(J, t0, t1, 0.0f, 0.0f, 0.0f, 0.0f, nullptr,
+            end0 + ((int64_t)blockIdx.y * chunks + c) * 4);
+}
+
+// Phase 2 and 3: each chunk forms its entry state from the zero-state ends
+// of the `depth` chunks before it (Horner in double) and re-runs from it.
+__global__ void k_iir_apply(const IirJob* __restrict__ jobs, const float* __restrict__ end0,
+                            int chunks) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= chunks) return;
+  const IirJob& J = jobs[blockIdx.y];
+  const int64_t t0 = (int64_t)c * kIirChunk;
+  if (t0 >= J.n) return;
+  const int64_t t1 = min(J.n, t0 + kIirChunk);
+  double st[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = min(J.depth, c); i >= 1; --i) {
+    const float* z = end0 + ((int64_t)blockIdx.y * chunks + (c - i)) * 4;
+    double nx[4];
+    for (int r = 0; r < 4; ++r)
+      nx[r] = J.mk[4 * r] * st[0] + J.mk[4 * r + 1] * st[1] + J.mk[4 * r + 2] * st[2] +
+              J.mk[4 * r + 3] * st[3] + (double)z[r];
+    for (int r = 0; r < 4; ++r) st[r] = nx[r];
+  }
+  iir_chunk(J, t0, t1, (float)st[0], (float)st[1], (float)st[2], (float)st[3], J.y, nullptr);
+}
+
+// M^kIirChunk for the feedback recurrence y_t = -b1 y1 - b2 y2 - b3 y3 -
+// b4 y4 acting on (y1, y2, y3, y4), by repeated squaring in double.
+void companion_power(const LrFilter& f, double* out) {
+  double m[16] = {-(double)f.b1, -(double)f.b2, -(double)f.b3, -(double)f.b4, 1, 0, 0, 0,
+                  0, 1, 0, 0, 0, 0, 1, 0};
+  double r[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  auto mul = [](const double* a, const double* b, double* c) {
+    double t[16];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        double v = 0;
+        for (int k = 0; k < 4; ++k) v += a[4 * i + k] * b[4 * k + j];
+        t[4 * i + j] = v;
+      }
+    std::memcpy(c, t, sizeof t);
+  };
+  for (int e = kIirChunk; e > 0; e >>= 1) {
+    if (e & 1) mul(r, m, r);
+    mul(m, m, m);
+  }
+  std::memcpy(out, r, sizeof r);
+}
+
+// Chunks back that an entry state needs: the smallest d with
+// |M^K|^d < 1e-12 (infinity norm), or -1 when more than 256 would be.  The
+// reference's FP32 coefficients (pi = 22/7, products near 1e30) put poles
+// outside the unit circle for crossovers below about 110 Hz: its filters
+// diverge there, and only the sequential evaluation reproduces them.
+int entry_depth(const double* mk) {
+  double nrm = 0;
+  for (int i = 0; i < 4; ++i)
+    nrm = std::max(nrm, std::fabs(mk[4 * i]) + std::fabs(mk[4 * i + 1]) + std::fabs(mk[4 * i + 2]) +
+                            std::fabs(mk[4 * i + 3]));
+  double p = 1.0;
+  for (int d = 1; d <= 256; ++d) {
+    p *= nrm;
+    if (p < 1e-12) return d;
+  }
+  return -1;
+}
+
 // ------------------------------------------------------ direct convolution
 
 // One context as the direct kernel reads it.  h(j) is the response at j for
@@ -674,7 +822,47 @@ ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3], 
     a.out[1] = d + 2 * n;
     a.out[2] = d + 3 * n;
   }
-  k_band_split<<<1, 32, 0, s>>>(a);
+  IirJob jobs[4];
+  bool chunked = (flags & EAR_SPLIT_CHUNKED) != 0;
+  if (chunked) {
+    // fall back to the sequential filters when a crossover is so low that
+    // the entry recurrence would need more than 256 chunks
+    for (int j = 0; j < 4 && chunked; ++j) {
+      companion_power(a.f[j], jobs[j].mk);
+      jobs[j].depth = entry_depth(jobs[j].mk);
+      chunked = jobs[j].depth > 0;
+    }
+  }
+  if (chunked) {
+    // low, high and LP2 (into the mid buffer) at once, then HP1 in place of
+    // it through a temporary copy of its input
+    const int chunks = (int)((n + kIirChunk - 1) / kIirChunk);
+    const size_t tabs = align256(sizeof(IirJob) * 4) + align256(sizeof(float) * 4 * 3 * chunks) +
+                        align256(sizeof(float) * (size_t)n);
+    CU(ensure(&sc.tab, &sc.tab_cap, tabs));
+    const float* src[4] = {a.x, a.x, a.x, nullptr};
+    float* dst[4] = {a.out[0], a.out[2], a.out[1], a.out[1]};
+    char* t = sc.tab;
+    IirJob* d_jobs = (IirJob*)t;
+    float* end0 = (float*)(t + align256(sizeof(IirJob) * 4));
+    float* tmp = (float*)((char*)end0 + align256(sizeof(float) * 4 * 3 * chunks));
+    src[3] = tmp;
+    for (int j = 0; j < 4; ++j) {
+      jobs[j].x = src[j];
+      jobs[j].y = dst[j];
+      jobs[j].n = n;
+      jobs[j].f = a.f[j];
+    }
+    CU(cudaMemcpyAsync(d_jobs, jobs, sizeof jobs, cudaMemcpyHostToDevice, s));
+    const dim3 g3((unsigned)((chunks + 63) / 64), 3), g1((unsigned)((chunks + 63) / 64), 1);
+    k_iir_zero<<<g3, 64, 0, s>>>(d_jobs, end0, chunks);
+    k_iir_apply<<<g3, 64, 0, s>>>(d_jobs, end0, chunks);
+    CU(cudaMemcpyAsync(tmp, a.out[1], sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    k_iir_zero<<<g1, 64, 0, s>>>(d_jobs + 3, end0, chunks);
+    k_iir_apply<<<g1, 64, 0, s>>>(d_jobs + 3, end0, chunks);
+  } else {
+    k_band_split<<<1, 32, 0, s>>>(a);
+  }
   CU(cudaGetLastError());
   if (!on_dev) {
     CU(cudaMemcpyAsync(low, a.out[0], sizeof(float) * n, cudaMemcpyDeviceToHost, s));

@@ -13,8 +13,10 @@
 // response window, default 8), --device N, --out DIR (where `render` also
 // writes the impulse responses when the file sets no debugdir), --conv
 // fft|direct (the convolution of the reference built with or without
-// FFTW; default fft), --dump-tracks DIR (also write the post-processed
-// tracks the convolution reads, with their bookkeeping).
+// FFTW; default fft), --split exact|chunked (the band split bit-identical
+// to the reference's sequential filters, the default, or parallel over
+// chunks), --dump-tracks DIR (also write the post-processed tracks the
+// convolution reads, with their bookkeeping).
 //
 // Render() of the reference (src/EAR.cpp:55-393) is followed step by step:
 // settings, the parse loop (the sources' WAVs are read and band-split
@@ -50,6 +52,7 @@ struct Options {
   unsigned long long seed = (unsigned long long)time(nullptr);
   bool exact = false;
   bool conv_direct = false;  // --conv direct: the reference built without FFTW
+  bool split_chunked = false;  // --split chunked: parallel band split
   std::string dump;          // --dump-tracks DIR
   double seconds = 8.0;
   int device = 0;
@@ -117,8 +120,8 @@ std::vector<DryBands> load_sources(const earfile::Scene& sc, const std::string& 
       if (!wav::read_float(resolve(fn, ear_path), &x)) throw CliError{"Failed to open sound file " + fn};
       for (int b = 0; b < 3; ++b) out[s].band[b].resize(x.size());
       if (ear_band_split(x.data(), (int64_t)x.size(), fr, out[s].band[0].data(),
-                         out[s].band[1].data(), out[s].band[2].data(), 0, nullptr,
-                         opt.device) != EAR_OK)
+                         out[s].band[1].data(), out[s].band[2].data(),
+                         opt.split_chunked ? EAR_SPLIT_CHUNKED : 0u, nullptr, opt.device) != EAR_OK)
         throw CliError{ear_last_error()};
     }
   }
@@ -628,6 +631,11 @@ int main(int argc, char** argv) {
       if (a == "--seed") opt.seed = std::stoull(value("--seed"));
       else if (a == "--exact") opt.exact = true;
       else if (a == "--dump-tracks") opt.dump = value("--dump-tracks");
+      else if (a == "--split") {
+        const std::string m = value("--split");
+        if (m != "exact" && m != "chunked") throw CliError{"--split takes exact or chunked"};
+        opt.split_chunked = m == "chunked";
+      }
       else if (a == "--conv") {
         const std::string m = value("--conv");
         if (m != "fft" && m != "direct") throw CliError{"--conv takes fft or direct"};
@@ -711,7 +719,7 @@ int main(int argc, char** argv) {
   }
   std::cout << "Usage:" << std::endl
             << " EAR render <filename> [--seed N] [--exact] [--seconds S] [--out DIR]"
-               " [--conv fft|direct]" << std::endl
+               " [--conv fft|direct] [--split exact|chunked]" << std::endl
             << " EAR calc T60 <filename> [--seed N] [--exact] [--seconds S]" << std::endl;
   return 1;
 }

@@ -449,7 +449,15 @@ ear_status ear_statistical_t60(const float* vertices,
    (f1+f2)/2 and (f2+f3)/2, with f = freq_khz * 1000 (the FREQ block; the
    reference's defaults are 0.2, 1.0 and 2.0 kHz, src/SoundFile.cpp:238-240).
    low = LP(x), high = HP(x), mid = HP(LP(x)) at the two crossovers.  The
-   results are bit-identical to the reference's sequential filters. */
+   results are bit-identical to the reference's sequential filters, which
+   run one sample after another.  With EAR_SPLIT_CHUNKED in `flags` the
+   filters run in parallel over chunks of 512 samples (a chunk's response
+   from a zero feedback state plus the propagated entry state): the first
+   chunk is bit-identical; after it the result keeps the accuracy of the
+   FP32 filters (the reference's own sequential FP32 output drifts up to
+   ~1e-3 of the peak from exact arithmetic in the low band) without their
+   exact rounding. */
+#define EAR_SPLIT_CHUNKED 2u
 ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3],
                           float* low, float* mid, float* high, uint32_t flags,
                           void* stream, int32_t device);
