@@ -561,6 +561,23 @@ __global__ void __launch_bounds__(256) k_fft_pass(const float2* __restrict__ in,
     for (int r = 1; r < R; ++r) a[r] = cmul(a[r], twiddle((uint32_t)(jm * r), log2ns + kLogR));
   }
   dft<R>(a);
+  if (log2ns == 0 && (stride & 255) == 0) {
+    // first pass: thread j writes outputs j*R .. j*R+R-1; staged through
+    // shared memory (rows padded to R+1) so that a warp's stores are
+    // contiguous instead of R-strided
+    __shared__ float2 s_t[256 * (R + 1)];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < R; ++r) s_t[t * (R + 1) + r] = a[r];
+    __syncthreads();
+    float2* o = out + base + (int64_t)blockIdx.x * 256 * R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int i = t + 256 * q;
+      o[i] = s_t[(i / R) * (R + 1) + (i % R)];
+    }
+    return;
+  }
   const int64_t d = ((j >> log2ns) << (log2ns + kLogR)) + jm;
 #pragma unroll
   for (int r = 0; r < R; ++r) out[base + d + r * ns] = a[r];
