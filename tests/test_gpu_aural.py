@@ -215,3 +215,22 @@ def test_full_size_fft_agrees_with_direct():
     peak = np.abs(d).max()
     assert np.abs(f - d).max() <= 1e-5 * peak
     assert st_d["multiply_adds"] >= 10 * 44100 * (4 * 44100 - 250)
+
+
+def test_fft_beyond_2_24_points_agrees_with_direct():
+    """A section of 2^24 + 100 samples with a 1 000-sample response needs a
+    2^25-point transform, whose twiddles are formed from a coarse and a fine
+    factor: it agrees with the exact direct sum within 1e-5 of the peak."""
+    import torch
+
+    rng = np.random.default_rng(25)
+    n = (1 << 24) + 100
+    ir = track(rng, 1000, 3, 990, 300.0)
+    dry = torch.from_numpy((rng.standard_normal(n) * 0.2).astype(np.float32)).cuda()
+    ctx = [Context(Track(torch.from_numpy(ir.data).cuda(), ir.first, ir.length), dry, 0)]
+    n_out = aural.processed_capacity(ctx[0], "fft")
+    f, st = aural.convolve(ctx, "fft", out_length=n_out)
+    d, _ = aural.convolve(ctx, "direct", out_length=n_out)
+    assert st["fft_points"] >= (1 << 25)
+    f, d = f.cpu().numpy(), d.cpu().numpy()
+    assert np.abs(f - d).max() <= 1e-5 * np.abs(d).max()
