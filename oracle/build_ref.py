@@ -46,4 +46,4 @@ def build(root: Path = DEFAULT_ROOT, force: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
-    print(build(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_ROOT, force=True))
+    print(build(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_ROOT))
