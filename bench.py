@@ -379,8 +379,8 @@ def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_c
 def auralisation(device: int, steps: int, cpu: bool):
     """The auralisation after the impulse responses (src/EAR.cpp:295-386) at
     the 10-track shape: 10 recorder tracks x 3 bands of 4 s responses
-    (176,400 samples) convolved with 10 s band sections, one ear_convolve
-    per track (3 contexts), as `EAR render` issues them; plus the band split
+    (176,400 samples) convolved with 10 s band sections, all 30 contexts in
+    one ear_convolve_tracks call, as `EAR render` issues them; plus the band split
     of the 10 s dry sound.  Inputs resident on the device (CUDA events on the
     stream); `e2e` repeats the FFT mode through host buffers.  The CPU legs
     time numpy's FFT convolution per context (the FFTW build's work, one
@@ -423,39 +423,42 @@ def auralisation(device: int, steps: int, cpu: bool):
         return e0.elapsed_time(e1) / n, r
 
     res = {"workload": "10 tracks x 3 bands: 4 s responses (176,400 samples) x 10 s sections "
-                       "(441,000 samples); one ear_convolve per track"}
+                       "(441,000 samples); one ear_convolve_tracks call for all tracks"}
     cap = {m: max(aural.processed_capacity(c, m) for c in host_ctx[0]) for m in ("fft", "direct")}
     outs = {m: [torch.zeros(cap[m], device=dev) for _ in range(tracks)] for m in cap}
     kstat = {}
 
+    flat = [c for row in dev_ctx for c in row]
+    track_of = [t for t in range(tracks) for _ in range(3)]
+
     def run(mode):
-        ks = 0.0
-        st = None
-        for t in range(tracks):
-            outs[mode][t].zero_()
-            _, st = aural.convolve(dev_ctx[t], mode, out=outs[mode][t])
-            ks += st["kernel_ms"]
-        kstat[mode] = (ks, st)
-        return ks
+        for o in outs[mode]:
+            o.zero_()
+        _, st = aural.convolve_tracks(flat, track_of, mode, outs=outs[mode])
+        kstat[mode] = (st["kernel_ms"], st)
+        return st["kernel_ms"]
 
     n = max(1, min(steps, 5))
     fft_ms, _ = timed(lambda: run("fft"), n)
     ks, st = kstat["fft"]
-    l = st["fft_points"] // 5  # 3 forward slots + 2 inverse pairs of one size
+    nctx = 3 * tracks
+    npair = (nctx + 1) // 2  # two contexts share one inverse transform
+    l = st["fft_points"] // (nctx + npair)  # one transform size for all
     npass = (int(l).bit_length() - 1 + 3) // 4
-    # algorithmic bytes of one track call: 16 B per point per radix pass over
-    # the 5 transforms, 8 B written per packed point + 8 B of inputs read,
-    # the product (2 x 8 B read per slot point, 8 B written per pair point)
-    # and the accumulate (8 B per result point + 8 B per output sample)
-    per_call = 16.0 * 5 * l * npass + (8 + 8) * 3 * l + 16 * 3 * l + 8 * 2 * l \
-        + 8.0 * 3 * (n_ir + n_dry) + 8.0 * cap["fft"]
+    # algorithmic bytes of the call: 16 B per point per radix pass over the
+    # forward and inverse transforms, 8 B written per packed point + 8 B of
+    # inputs read, the product (2 x 8 B read per slot point, 8 B written per
+    # pair point) and the accumulate (8 B per result point + 8 B per output
+    # sample)
+    per_call = 16.0 * (nctx + npair) * l * npass + (8 + 8) * nctx * l + 16 * nctx * l \
+        + 8 * npair * l + 8.0 * nctx * (n_ir + n_dry) + 8.0 * tracks * cap["fft"]
     hbm, src = peaks()
-    ach = per_call * tracks / (ks / 1000.0) / 1e9
+    ach = per_call / (ks / 1000.0) / 1e9
     res["fft"] = {"ms": fft_ms, "kernel_ms": ks, "contexts_per_s": 3 * tracks / (fft_ms / 1000.0),
                   "transform_points": int(l), "passes": npass,
                   "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                                "frac": ach / hbm, "peak_source": src,
-                               "note": "one call's transforms (5 x 8 MB) stay L2-resident"}}
+                               "note": "45 transforms of 8 MB: partly L2-resident"}}
     dir_ms, _ = timed(lambda: run("direct"), 1)
     ks, st = kstat["direct"]
     macs = float(st["multiply_adds"]) * tracks
@@ -470,9 +473,10 @@ def auralisation(device: int, steps: int, cpu: bool):
                          "note": "sequential: bit-identical; chunked: parallel over 512-sample "
                                  "chunks, FP32-filter accuracy"}
     # e2e: host buffers, copies inside the call
+    hflat = [c for row in host_ctx for c in row]
+    aural.convolve_tracks(hflat, track_of, "fft", out_lengths=[cap["fft"]] * tracks)  # warm-up
     t0 = time.perf_counter()
-    for t in range(tracks):
-        aural.convolve(host_ctx[t], "fft", out_length=cap["fft"])
+    aural.convolve_tracks(hflat, track_of, "fft", out_lengths=[cap["fft"]] * tracks)
     e2e_ms = (time.perf_counter() - t0) * 1000.0
     res["e2e"] = {"fft_ms": e2e_ms, "h2d_bytes": 4 * (3 * tracks * n_ir + n_dry),
                   "d2h_bytes": 4 * tracks * cap["fft"]}

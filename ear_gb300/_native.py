@@ -183,6 +183,9 @@ SIGNATURES = {
     "ear_convolve": (C.c_int, [C.POINTER(EarConvContext), C.c_int32, C.c_int32, C.c_void_p,
                                C.c_int64, C.c_uint32, C.c_void_p, C.c_int32,
                                C.POINTER(EarConvStats)]),
+    "ear_convolve_tracks": (C.c_int, [C.POINTER(EarConvContext), C.c_void_p, C.c_int32, C.c_int32,
+                                      C.c_void_p, C.c_void_p, C.c_int32, C.c_uint32, C.c_void_p,
+                                      C.c_int32, C.POINTER(EarConvStats)]),
     "ear_conv_processed_capacity": (C.c_int64, [C.POINTER(EarConvContext), C.c_int32]),
     "ear_conv_processed_length": (C.c_int64, [C.POINTER(EarConvContext), C.c_int32]),
 }

@@ -190,3 +190,53 @@ def convolve(contexts: Sequence[Context], mode: str = "fft", out=None, out_lengt
     stats = {"kernel_ms": st.kernel_ms, "launches": st.launches, "fft_points": st.fft_points,
              "multiply_adds": st.multiply_adds}
     return out, stats
+
+
+def convolve_tracks(contexts: Sequence[Context], tracks: Sequence[int], mode: str = "fft",
+                    outs=None, out_lengths=None, device: int = 0):
+    """``convolve`` for several output tracks in one call: context i is added
+    to output track ``tracks[i]`` (each track's contexts in their order).
+    ``outs`` (optional) are added to; by default zero tracks whose lengths
+    (``out_lengths``, default: each track's largest processed capacity) are
+    as ``convolve`` picks them.  Returns (list of outputs, stats)."""
+    if mode not in MODES:
+        raise ValueError(f"mode must be one of {sorted(MODES)}")
+    if len(tracks) != len(contexts):
+        raise ValueError("one track index per context")
+    num_tracks = (max(tracks) + 1 if len(tracks) else 0) if outs is None else len(outs)
+    keep: list = []
+    arr = (N.EarConvContext * max(len(contexts), 1))()
+    for i, c in enumerate(contexts):
+        arr[i] = _c_context(c, keep)
+    L = N.lib()
+    if out_lengths is None:
+        out_lengths = [0] * num_tracks
+        for i, t in enumerate(tracks):
+            out_lengths[t] = max(out_lengths[t],
+                                 int(L.ear_conv_processed_capacity(C.byref(arr[i]), MODES[mode])))
+    on_dev = any(_is_cuda_tensor(x) for x in keep)
+    if outs is None:
+        if on_dev:
+            import torch
+
+            dev = next(x.device for x in keep if _is_cuda_tensor(x))
+            outs = [torch.zeros(int(n), dtype=torch.float32, device=dev) for n in out_lengths]
+        else:
+            outs = [np.zeros(int(n), np.float32) for n in out_lengths]
+    if on_dev and not all(_is_cuda_tensor(x) for x in list(keep) + list(outs)):
+        raise TypeError("mix of host and device buffers: pass all numpy or all CUDA tensors")
+    tr = np.ascontiguousarray(np.asarray(tracks, np.int32))
+    ptrs = (C.c_void_p * max(num_tracks, 1))(*[_ptr(o) or None for o in outs])
+    lens = (C.c_int64 * max(num_tracks, 1))(*[int(len(o)) for o in outs])
+    st = N.EarConvStats()
+    if on_dev:
+        dev_index = next(x.device for x in keep if _is_cuda_tensor(x)).index or 0
+        N.check(L.ear_convolve_tracks(arr, tr.ctypes.data, len(contexts), MODES[mode], ptrs, lens,
+                                      num_tracks, N.EAR_AURAL_DEVICE_MEMORY, _stream_of(outs[0]),
+                                      dev_index, C.byref(st)))
+    else:
+        N.check(L.ear_convolve_tracks(arr, tr.ctypes.data, len(contexts), MODES[mode], ptrs, lens,
+                                      num_tracks, 0, None, device, C.byref(st)))
+    stats = {"kernel_ms": st.kernel_ms, "launches": st.launches, "fft_points": st.fft_points,
+             "multiply_adds": st.multiply_adds}
+    return list(outs), stats

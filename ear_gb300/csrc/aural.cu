@@ -418,7 +418,15 @@ __device__ __forceinline__ void direct_context(const DirectCtx& C, int64_t x0, i
   }
 }
 
-// One block: kDirTile consecutive outputs.  For each context in order its
+// One output track and its contexts [begin, end) of the context table.
+struct OutTrack {
+  float* out;
+  int64_t len;
+  int begin, end;
+};
+
+// One block: kDirTile consecutive samples of output track blockIdx.y.  For
+// each of the track's contexts in order its
 // own sum t[x] is accumulated from +0 in ascending i and then added to the
 // total, as RecorderTrack::Process and Recorder::Add do.  Terms outside a
 // context's range read zero-padded dry or response samples and add +-0,
@@ -426,20 +434,23 @@ __device__ __forceinline__ void direct_context(const DirectCtx& C, int64_t x0, i
 // keyframe-interpolation path in as well.
 template <bool ANY_INTERP>
 __global__ void __launch_bounds__(kDirThreads) k_conv_direct(const DirectCtx* __restrict__ ctxs,
-                                                             int num_ctx, float* __restrict__ out,
-                                                             int64_t out_len) {
+                                                             const OutTrack* __restrict__ tracks) {
   using SH = DirShape<ANY_INTERP>;
   constexpr int kDirR = SH::R, kDirTile = SH::Tile, kDirChunk = SH::Chunk, kDirWin = SH::Win;
   __shared__ float s_dry[kDirChunk];
   __shared__ float s_h[kDirWin];
   __shared__ float s_h2[ANY_INTERP ? kDirWin : 1];
+  const OutTrack T = tracks[blockIdx.y];
+  float* __restrict__ out = T.out;
+  const int64_t out_len = T.len;
   const int t = threadIdx.x;
   const int64_t x0 = (int64_t)blockIdx.x * kDirTile;
+  if (x0 >= out_len) return;  // block-uniform: this track is shorter
   const int64_t xt = x0 + (int64_t)t * kDirR;
   float total[kDirR];
 #pragma unroll
   for (int r = 0; r < kDirR; ++r) total[r] = xt + r < out_len ? out[xt + r] : 0.0f;
-  for (int c = 0; c < num_ctx; ++c) {
+  for (int c = T.begin; c < T.end; ++c) {
     const DirectCtx C = ctxs[c];
     if (C.len <= C.first || C.n <= 0) continue;
     if (x0 + kDirTile - 1 < C.off + C.first || x0 > C.off + C.n - 1 + C.len - 1) continue;
@@ -672,12 +683,15 @@ struct FftOut {
   int imag;
 };
 
-__global__ void k_fft_accumulate(const FftOut* __restrict__ outs, int num, float* __restrict__ out,
-                                 int64_t x0, int64_t x1) {
-  const int64_t x = x0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= x1) return;
+// Output track blockIdx.y: its contexts' processed tracks added in order.
+__global__ void k_fft_accumulate(const FftOut* __restrict__ outs,
+                                 const OutTrack* __restrict__ tracks) {
+  const OutTrack T = tracks[blockIdx.y];
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= T.len) return;
+  float* out = T.out;
   float acc = out[x];
-  for (int c = 0; c < num; ++c) {
+  for (int c = T.begin; c < T.end; ++c) {
     const FftOut O = outs[c];
     const int64_t u = x - O.off;
     if (u < 0 || u >= O.mn) continue;
@@ -893,14 +907,32 @@ ear_status ear_band_split(const float* dry, int64_t n, const float freq_khz[3], 
 ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t mode, float* out,
                         int64_t out_length, uint32_t flags, void* stream, int32_t device,
                         ear_conv_stats* stats) {
+  return ear_convolve_tracks(contexts, nullptr, num, mode, &out, &out_length, 1, flags, stream,
+                             device, stats);
+}
+
+ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* context_track,
+                               int32_t num, int32_t mode, float* const* outs,
+                               const int64_t* out_lengths, int32_t num_tracks, uint32_t flags,
+                               void* stream, int32_t device, ear_conv_stats* stats) {
   if (stats) std::memset(stats, 0, sizeof *stats);
-  if (num < 0 || (num > 0 && !contexts) || out_length < 0 || (out_length > 0 && !out))
+  if (num < 0 || (num > 0 && !contexts) || num_tracks < 1 || num_tracks > 65535 || !outs ||
+      !out_lengths || (num_tracks > 1 && num > 0 && !context_track))
     return fail(EAR_ERR_INVALID_ARG, "ear_convolve: bad arguments");
   if (mode != EAR_CONV_FFT && mode != EAR_CONV_DIRECT)
     return fail(EAR_ERR_INVALID_ARG, "ear_convolve: unknown mode %d", mode);
-  for (int i = 0; i < num; ++i)
+  for (int o = 0; o < num_tracks; ++o)
+    if (out_lengths[o] < 0 || (out_lengths[o] > 0 && !outs[o]))
+      return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output track %d is invalid", o);
+  for (int i = 0; i < num; ++i) {
     if (!check_context(contexts[i], i)) return EAR_ERR_INVALID_ARG;
-  if (num == 0 || out_length == 0) return EAR_OK;
+    if (context_track && (context_track[i] < 0 || context_track[i] >= num_tracks))
+      return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d names track %d of %d", i,
+                  context_track ? context_track[i] : 0, num_tracks);
+  }
+  int64_t max_len = 0;
+  for (int o = 0; o < num_tracks; ++o) max_len = std::max(max_len, out_lengths[o]);
+  if (num == 0 || max_len == 0) return EAR_OK;
   CU(cudaSetDevice(device));
   const bool on_dev = flags & EAR_AURAL_DEVICE_MEMORY;
   cudaStream_t s = on_dev ? (cudaStream_t)stream : nullptr;
@@ -914,7 +946,25 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
   // ---- stage the caller's buffers (host calls): one device arena, each
   // distinct host buffer copied once (a response serves as this keyframe's
   // and the previous keyframe's partner; a band serves every recorder)
-  std::vector<ear_conv_context> ctx(contexts, contexts + num);
+  // contexts grouped by output track, each track's in the caller's order
+  std::vector<int> order(num);
+  for (int i = 0; i < num; ++i) order[i] = i;
+  if (context_track)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return context_track[x] < context_track[y]; });
+  std::vector<ear_conv_context> ctx(num);
+  std::vector<OutTrack> tracks(num_tracks);
+  for (int o = 0; o < num_tracks; ++o) tracks[o] = OutTrack{outs[o], out_lengths[o], 0, 0};
+  std::vector<char> seen(num_tracks, 0);
+  for (int k = 0; k < num; ++k) {
+    ctx[k] = contexts[order[k]];
+    const int o = context_track ? context_track[order[k]] : 0;
+    if (!seen[o]) {
+      tracks[o].begin = k;
+      seen[o] = 1;
+    }
+    tracks[o].end = k + 1;
+  }
   size_t staged = 0;
   auto ir_need = [](const ear_conv_context& c) {
     return std::max(c.ir_length, c.ir_next ? c.ir_next_length : (int64_t)0);
@@ -937,7 +987,13 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       at[kv.first] = staged;
       staged += align256(sizeof(float) * (size_t)kv.second);
     }
-    staged += align256(sizeof(float) * out_length);
+  }
+  std::vector<size_t> at_out(num_tracks, 0);
+  if (!on_dev) {
+    for (int o = 0; o < num_tracks; ++o) {
+      at_out[o] = staged;
+      staged += align256(sizeof(float) * (size_t)out_lengths[o]);
+    }
   }
 
   // ---- mode-specific scratch layout
@@ -986,7 +1042,6 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
   const size_t total_bytes = staged + ramp_bytes + fft_bytes;
   if (total_bytes > 0) CU(ensure(&sc.buf, &sc.cap, total_bytes));
   char* arena = sc.buf;
-  float* d_out = out;
   if (!on_dev) {
     for (const auto& kv : spans)
       CU(cudaMemcpyAsync(arena + at[kv.first], kv.first, sizeof(float) * kv.second,
@@ -1007,8 +1062,12 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       if (!c.ir) c.ir_capacity = 0;
       c.dry = dev(c.dry);
     }
-    d_out = (float*)(arena + staged - align256(sizeof(float) * out_length));
-    CU(cudaMemcpyAsync(d_out, out, sizeof(float) * out_length, cudaMemcpyHostToDevice, s));
+    for (int o = 0; o < num_tracks; ++o) {
+      tracks[o].out = (float*)(arena + at_out[o]);
+      if (out_lengths[o] > 0)
+        CU(cudaMemcpyAsync(tracks[o].out, outs[o], sizeof(float) * out_lengths[o],
+                           cudaMemcpyHostToDevice, s));
+    }
   }
   char* fft_arena = arena + staged + ramp_bytes;
   float* ramps = (float*)(arena + staged);
@@ -1046,16 +1105,19 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       if (d.len > d.first && d.n > 0) macs += (double)d.n * (double)(d.len - d.first);
     }
     const size_t at = push(dc.data(), sizeof(DirectCtx) * num);
+    const size_t at_t = push(tracks.data(), sizeof(OutTrack) * num_tracks);
     CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
     CU(cudaMemcpyAsync(sc.tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
     const DirectCtx* d_ctx = (const DirectCtx*)(sc.tab + at);
+    const OutTrack* d_tracks = (const OutTrack*)(sc.tab + at_t);
     const int tile = any_interp ? DirShape<true>::Tile : DirShape<false>::Tile;
-    const int64_t blocks = (out_length + tile - 1) / tile;
+    const int64_t blocks = (max_len + tile - 1) / tile;
     if (blocks > 0x7fffffffLL) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output too long");
+    const dim3 grid((unsigned)blocks, (unsigned)num_tracks);
     if (any_interp)
-      k_conv_direct<true><<<(unsigned)blocks, kDirThreads, 0, s>>>(d_ctx, num, d_out, out_length);
+      k_conv_direct<true><<<grid, kDirThreads, 0, s>>>(d_ctx, d_tracks);
     else
-      k_conv_direct<false><<<(unsigned)blocks, kDirThreads, 0, s>>>(d_ctx, num, d_out, out_length);
+      k_conv_direct<false><<<grid, kDirThreads, 0, s>>>(d_ctx, d_tracks);
     ++launches;
     CU(cudaGetLastError());
   } else {
@@ -1072,8 +1134,7 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
     if (!fr.empty()) at_fr = push(fr.data(), sizeof(FadeRamp) * fr.size());
     // per group: slots, pairs; then the outputs in context order
     std::vector<size_t> at_slots(groups.size()), at_pairs(groups.size());
-    std::vector<FftOut> outs(num);
-    std::vector<int> final_in_a(groups.size());
+    std::vector<FftOut> couts(num);
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group& g = groups[gi];
       std::vector<FftSlot> slots(g.slots);
@@ -1100,7 +1161,8 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       at_slots[gi] = push(slots.data(), sizeof(FftSlot) * slots.size());
       at_pairs[gi] = push(pairs.data(), sizeof(FftPair) * pairs.size());
     }
-    const size_t at_outs_placeholder = push(outs.data(), sizeof(FftOut) * num);
+    const size_t at_outs_placeholder = push(couts.data(), sizeof(FftOut) * num);
+    const size_t at_tracks = push(tracks.data(), sizeof(OutTrack) * num_tracks);
     CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
     char* dtab = sc.tab;
     if (!fr.empty()) {
@@ -1148,20 +1210,20 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       points += l * (int64_t)(g.slots + g.pairs);
       for (int p = 0; p < g.pairs; ++p) {
         const int ia = g.jobs[2 * p];
-        outs[ia] = FftOut{inv + (int64_t)p * l, ctx[ia].offset,
+        couts[ia] = FftOut{inv + (int64_t)p * l, ctx[ia].offset,
                           std::max(ctx[ia].ir_length, ctx[ia].ir_next ? ctx[ia].ir_next_length : 0) +
                               ctx[ia].dry_length + 1,
                           0};
         if (2 * p + 1 < (int)g.jobs.size()) {
           const int ib = g.jobs[2 * p + 1];
-          outs[ib] = FftOut{inv + (int64_t)p * l, ctx[ib].offset,
+          couts[ib] = FftOut{inv + (int64_t)p * l, ctx[ib].offset,
                             std::max(ctx[ib].ir_length, ctx[ib].ir_next ? ctx[ib].ir_next_length : 0) +
                                 ctx[ib].dry_length + 1,
                             1};
         }
       }
     }
-    std::memcpy(tab.data() + at_outs_placeholder, outs.data(), sizeof(FftOut) * num);
+    std::memcpy(tab.data() + at_outs_placeholder, couts.data(), sizeof(FftOut) * num);
     CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
     if (!fr.empty()) {
       k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, s>>>((const FadeRamp*)(dtab + at_fr), (int)fr.size());
@@ -1185,13 +1247,17 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num, int32_t m
       if (v != pair_result[gi])
         return fail(EAR_ERR_STATE, "ear_convolve: internal buffer plan mismatch");
     }
-    k_fft_accumulate<<<(unsigned)((out_length + 255) / 256), 256, 0, s>>>(
-        (const FftOut*)(dtab + at_outs_placeholder), num, d_out, 0, out_length);
+    k_fft_accumulate<<<dim3((unsigned)((max_len + 255) / 256), (unsigned)num_tracks), 256, 0, s>>>(
+        (const FftOut*)(dtab + at_outs_placeholder), (const OutTrack*)(dtab + at_tracks));
     ++launches;
     CU(cudaGetLastError());
   }
   CU(cudaEventRecord(sc.ev[1], s));
-  if (!on_dev) CU(cudaMemcpyAsync(out, d_out, sizeof(float) * out_length, cudaMemcpyDeviceToHost, s));
+  if (!on_dev)
+    for (int o = 0; o < num_tracks; ++o)
+      if (out_lengths[o] > 0)
+        CU(cudaMemcpyAsync(outs[o], tracks[o].out, sizeof(float) * out_lengths[o],
+                           cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   if (stats) {
     float ms = 0;

@@ -253,48 +253,57 @@ void auralise(const earfile::Scene& sc, const std::vector<Context>& contexts, in
     }
   }
   std::cout << "Merging result..." << std::endl;
+  // every track of every recorder in one call: context lists per track
+  int num_tracks = 0;
+  for (const auto& r : sc.recorders) num_tracks += r.channels;
+  std::vector<ear_conv_context> cs;
+  std::vector<int32_t> track_of;
+  std::vector<int64_t> cap((size_t)num_tracks, 0);
+  for (int t = 0; t < num_tracks; ++t)
+    for (const Item& it : items) {
+      cs.push_back(ctx_of(it, t));
+      track_of.push_back(t);
+      cap[(size_t)t] = std::max(cap[(size_t)t], ear_conv_processed_capacity(&cs.back(), mode));
+    }
+  std::vector<std::vector<float>> out((size_t)num_tracks);
+  std::vector<float*> ptr((size_t)num_tracks);
+  for (int t = 0; t < num_tracks; ++t) {
+    out[(size_t)t].assign((size_t)cap[(size_t)t], 0.0f);
+    ptr[(size_t)t] = out[(size_t)t].data();
+  }
+  ear_conv_stats st = {};
+  if (ear_convolve_tracks(cs.data(), track_of.data(), (int32_t)cs.size(), mode, ptr.data(),
+                          cap.data(), num_tracks, 0, nullptr, opt.device, &st) != EAR_OK)
+    throw CliError{ear_last_error()};
+  gpu_ms += st.kernel_ms;
+  ++conv_calls;
   int t0 = 0;
   for (size_t ri = 0; ri < sc.recorders.size(); ++ri) {
     const earfile::Recorder& rec = sc.recorders[ri];
     const int ch = rec.channels;
-    std::vector<std::vector<float>> out((size_t)ch);
+    // Recorder::Add reads each processed track over its capacity: the sum
+    // ends at index cap - 1 (its real_length)
     std::vector<int> real((size_t)ch);
-    for (int k = 0; k < ch; ++k) {
-      std::vector<ear_conv_context> cs;
-      int64_t cap = 0;
-      for (const Item& it : items) {
-        cs.push_back(ctx_of(it, t0 + k));
-        cap = std::max(cap, ear_conv_processed_capacity(&cs.back(), mode));
-      }
-      out[(size_t)k].assign((size_t)cap, 0.0f);
-      ear_conv_stats st = {};
-      if (ear_convolve(cs.data(), (int32_t)cs.size(), mode, out[(size_t)k].data(), cap, 0, nullptr,
-                       opt.device, &st) != EAR_OK)
-        throw CliError{ear_last_error()};
-      gpu_ms += st.kernel_ms;
-      ++conv_calls;
-      // Recorder::Add reads each processed track over its capacity: the sum
-      // ends at index cap - 1 (its real_length)
-      real[(size_t)k] = (int)(cap - 1);
-    }
+    for (int k = 0; k < ch; ++k) real[(size_t)k] = (int)(cap[(size_t)(t0 + k)] - 1);
     // Recorder::Normalize(0.8) over the processed tracks
     // (src/Recorder.cpp:443-460, FloatBuffer::Maximum / Multiply)
     float max = -1e9f;
     for (int k = 0; k < ch; ++k) {
+      const std::vector<float>& o = out[(size_t)(t0 + k)];
       float x = 0.0f;
-      for (int i = 0; i < real[(size_t)k]; ++i) x = std::max(x, std::fabs(out[(size_t)k][(size_t)i]));
+      for (int i = 0; i < real[(size_t)k]; ++i) x = std::max(x, std::fabs(o[(size_t)i]));
       max = std::max(max, x);
     }
     if (max > 0.0f) {
       const float f = 0.8f / max;
       for (int k = 0; k < ch; ++k)
-        for (int i = 0; i < real[(size_t)k]; ++i) out[(size_t)k][(size_t)i] *= f;
+        for (int i = 0; i < real[(size_t)k]; ++i) out[(size_t)(t0 + k)][(size_t)i] *= f;
     }
-    std::vector<const float*> ptr;
-    for (int k = 0; k < ch; ++k) ptr.push_back(out[(size_t)k].data());
-    if (!wav::write(rec.filename, ptr, real, false, 1.0f)) throw CliError{"cannot write " + rec.filename};
-    std::cout << " " << rec.filename << ": " << ch << " channel(s), " << *std::max_element(real.begin(), real.end())
-              << " samples" << std::endl;
+    std::vector<const float*> chans;
+    for (int k = 0; k < ch; ++k) chans.push_back(out[(size_t)(t0 + k)].data());
+    if (!wav::write(rec.filename, chans, real, false, 1.0f)) throw CliError{"cannot write " + rec.filename};
+    std::cout << " " << rec.filename << ": " << ch << " channel(s), "
+              << *std::max_element(real.begin(), real.end()) << " samples" << std::endl;
     t0 += ch;
   }
   std::cout << " convolution (" << (opt.conv_direct ? "direct" : "fft") << "): " << items.size()

@@ -514,6 +514,18 @@ ear_status ear_convolve(const ear_conv_context* contexts, int32_t num_contexts,
                         uint32_t flags, void* stream, int32_t device,
                         ear_conv_stats* stats);
 
+/* ear_convolve for several output tracks in one call (e.g. every track of
+   every recorder): context i is added to output track context_track[i]
+   (NULL: all to track 0), each track's contexts in their order in the
+   array.  outs[t] holds out_lengths[t] samples.  Host buffers shared by
+   several contexts are copied to the device once.  At most 65535 tracks. */
+ear_status ear_convolve_tracks(const ear_conv_context* contexts,
+                               const int32_t* context_track, int32_t num_contexts,
+                               int32_t mode, float* const* outs,
+                               const int64_t* out_lengths, int32_t num_tracks,
+                               uint32_t flags, void* stream, int32_t device,
+                               ear_conv_stats* stats);
+
 /* The FloatBuffer capacity (src/Recorder.cpp:33-59, INITIAL 3 s, growth by
    1 s: src/Recorder.h:36-37) of the track RecorderTrack::Process returns for
    one context in `mode`.  Recorder::Add reads that many samples, so the

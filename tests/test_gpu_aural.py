@@ -234,3 +234,43 @@ def test_fft_beyond_2_24_points_agrees_with_direct():
     assert st["fft_points"] >= (1 << 25)
     f, d = f.cpu().numpy(), d.cpu().numpy()
     assert np.abs(f - d).max() <= 1e-5 * np.abs(d).max()
+
+
+@pytest.mark.parametrize("mode", ["direct", "fft"])
+def test_several_tracks_in_one_call_equal_separate_calls(mode):
+    """ear_convolve_tracks with the contexts of three output tracks given
+    interleaved equals one ear_convolve per track: bit for bit in direct
+    mode; in FFT mode within the FFT tolerance (two contexts share one
+    inverse transform, and which two depends on the call, so the last bits
+    may differ).  Host and device buffers give the same bits."""
+    import torch
+
+    rng = np.random.default_rng(31)
+    per_track = [contexts_case("offsets", rng), contexts_case("pairs", rng),
+                 contexts_case("single", rng)]
+    flat, track_of = [], []
+    for i in range(max(len(p) for p in per_track)):  # interleave the tracks' contexts
+        for t, p in enumerate(per_track):
+            if i < len(p):
+                flat.append(p[i])
+                track_of.append(t)
+    outs, st = aural.convolve_tracks(flat, track_of, mode)
+    assert len(outs) == 3
+    for t, p in enumerate(per_track):
+        ref, _ = aural.convolve(p, mode, out_length=len(outs[t]))
+        if mode == "direct":
+            np.testing.assert_array_equal(bits(outs[t]), bits(ref))
+        else:
+            peak = np.abs(ref).max()
+            assert np.abs(outs[t] - ref).max() <= FFT_TOL * peak
+
+    def dev(c):
+        return Context(Track(torch.from_numpy(c.ir.data).cuda(), c.ir.first, c.ir.length),
+                       torch.from_numpy(np.ascontiguousarray(c.dry)).cuda(), c.offset,
+                       None if c.ir_next is None else
+                       Track(torch.from_numpy(c.ir_next.data).cuda(), c.ir_next.first,
+                             c.ir_next.length))
+
+    douts, _ = aural.convolve_tracks([dev(c) for c in flat], track_of, mode)
+    for t in range(3):
+        np.testing.assert_array_equal(bits(outs[t]), bits(douts[t].cpu().numpy()))
