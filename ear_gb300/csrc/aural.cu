@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -704,6 +705,16 @@ __global__ void k_fft_accumulate(const FftOut* __restrict__ outs,
 // ------------------------------------------------------------ host side
 
 constexpr int64_t kInitialCapacity = 3 * 44100;  // INITIAL_BUFFER_SIZE, src/Recorder.h:36
+// Transform scratch per chunk of contexts: 4 GiB, or EAR_FFT_CHUNK_BYTES
+// from the environment (tests use it to force several chunks).
+size_t fft_budget() {
+  const char* e = std::getenv("EAR_FFT_CHUNK_BYTES");
+  if (e && *e) {
+    const unsigned long long v = std::strtoull(e, nullptr, 10);
+    if (v > 0) return (size_t)v;
+  }
+  return (size_t)4 << 30;
+}
 constexpr int64_t kIncrement = 44100;            // INCREMENTAL_BUFFER_SIZE, src/Recorder.h:37
 
 // FloatBuffer capacity after writes that start at index a and then never
@@ -1003,8 +1014,16 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
     int slots = 0, pairs = 0;
     size_t at_a = 0, at_b = 0;
   };
-  std::vector<Group> groups;
-  std::vector<int> slot0(num, -1), nslot(num, 0);
+  // FFT scratch is bounded: contexts run in chunks (in their sorted order)
+  // whose transforms fit fft_budget(); each chunk adds its contexts to the
+  // outputs in order, so the sums keep the order of one pass
+  struct Chunk {
+    int begin, end;
+    std::vector<Group> groups;
+    size_t bytes = 0;
+  };
+  std::vector<Chunk> chunks;
+  std::vector<int> slot0(num, -1), nslot(num, 0), log2l_of(num, 0);
   size_t fft_bytes = 0, ramp_bytes = 0;
   std::vector<size_t> at_ramp(num, 0);
   if (mode == EAR_CONV_FFT) {
@@ -1012,31 +1031,51 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
       const ear_conv_context& c = ctx[i];
       int64_t mn = c.ir_length + c.dry_length + 1;
       if (c.ir_next) mn = std::max(mn, c.ir_next_length + c.dry_length + 1);
-      const int lg = std::max(4, log2_ceil(mn));
-      if (lg > 30) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d needs a 2^%d transform", i, lg);
-      auto it = std::find_if(groups.begin(), groups.end(), [&](const Group& g) { return g.log2l == lg; });
-      if (it == groups.end()) {
-        groups.push_back(Group{lg, {}, 0, 0, 0, 0});
-        it = groups.end() - 1;
-      }
-      it->jobs.push_back(i);
+      log2l_of[i] = std::max(4, log2_ceil(mn));
+      if (log2l_of[i] > 30)
+        return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d needs a 2^%d transform", i,
+                    log2l_of[i]);
       nslot[i] = c.ir_next ? 2 : 1;
       if (c.ir_next && c.dry_length > 0) {
         at_ramp[i] = ramp_bytes;
         ramp_bytes += align256(sizeof(float) * 2 * (size_t)c.dry_length);
       }
     }
-    for (Group& g : groups) {
-      for (int i : g.jobs) {
-        slot0[i] = g.slots;
-        g.slots += nslot[i];
+    size_t run = 0;
+    const size_t budget = fft_budget();
+    for (int i = 0; i < num; ++i) {
+      // forward slots in A, pair results in B: about 2.5 transforms a slot
+      const size_t est = sizeof(float2) * ((size_t)5 * nslot[i] / 2 + 1) << log2l_of[i];
+      if (chunks.empty() || (run + est > budget && chunks.back().end > chunks.back().begin)) {
+        chunks.push_back(Chunk{i, i, {}, 0});
+        run = 0;
       }
-      g.pairs = ((int)g.jobs.size() + 1) / 2;
-      const size_t l = (size_t)1 << g.log2l;
-      g.at_a = fft_bytes;
-      fft_bytes += align256(sizeof(float2) * l * (size_t)g.slots);
-      g.at_b = fft_bytes;
-      fft_bytes += align256(sizeof(float2) * l * (size_t)std::max(g.slots, g.pairs));
+      run += est;
+      chunks.back().end = i + 1;
+    }
+    for (Chunk& ch : chunks) {
+      for (int i = ch.begin; i < ch.end; ++i) {
+        auto it = std::find_if(ch.groups.begin(), ch.groups.end(),
+                               [&](const Group& g) { return g.log2l == log2l_of[i]; });
+        if (it == ch.groups.end()) {
+          ch.groups.push_back(Group{log2l_of[i], {}, 0, 0, 0, 0});
+          it = ch.groups.end() - 1;
+        }
+        it->jobs.push_back(i);
+      }
+      for (Group& g : ch.groups) {
+        for (int i : g.jobs) {
+          slot0[i] = g.slots;
+          g.slots += nslot[i];
+        }
+        g.pairs = ((int)g.jobs.size() + 1) / 2;
+        const size_t l = (size_t)1 << g.log2l;
+        g.at_a = ch.bytes;
+        ch.bytes += align256(sizeof(float2) * l * (size_t)g.slots);
+        g.at_b = ch.bytes;
+        ch.bytes += align256(sizeof(float2) * l * (size_t)std::max(g.slots, g.pairs));
+      }
+      fft_bytes = std::max(fft_bytes, ch.bytes);
     }
   }
   const size_t total_bytes = staged + ramp_bytes + fft_bytes;
@@ -1121,7 +1160,7 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
     ++launches;
     CU(cudaGetLastError());
   } else {
-    // fade ramps of keyframe pairs
+    // fade ramps of keyframe pairs (every chunk's), one table at the front
     std::vector<FadeRamp> fr;
     for (int i = 0; i < num; ++i) {
       const ear_conv_context& c = ctx[i];
@@ -1130,46 +1169,88 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
       fr.push_back(FadeRamp{r, c.dry_length, 0});
       fr.push_back(FadeRamp{r + c.dry_length, c.dry_length, 1});
     }
-    size_t at_fr = 0;
-    if (!fr.empty()) at_fr = push(fr.data(), sizeof(FadeRamp) * fr.size());
-    // per group: slots, pairs; then the outputs in context order
-    std::vector<size_t> at_slots(groups.size()), at_pairs(groups.size());
-    std::vector<FftOut> couts(num);
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      Group& g = groups[gi];
-      std::vector<FftSlot> slots(g.slots);
-      for (int i : g.jobs) {
-        const ear_conv_context& c = ctx[i];
-        const float* ra = c.ir_next && c.dry_length > 0 ? (float*)((char*)ramps + at_ramp[i]) : nullptr;
-        FftSlot& a = slots[slot0[i]];
-        a = FftSlot{c.ir, c.dry, ra, c.ir ? c.ir_capacity : 0, c.ir_length, c.dry_length};
-        if (c.ir_next) {
-          slots[slot0[i] + 1] = FftSlot{c.ir_next, c.dry, ra ? ra + c.dry_length : nullptr,
-                                        c.ir_next_capacity, c.ir_next_length, c.dry_length};
+    if (!fr.empty()) push(fr.data(), sizeof(FadeRamp) * fr.size());
+    const size_t chunk_tab0 = align256(tab.size());
+    // per chunk: slot and pair tables of its groups, its contexts' results
+    // and the output tracks restricted to its contexts
+    struct ChunkTabs {
+      std::vector<char> tab;
+      std::vector<size_t> at_slots, at_pairs;
+      size_t at_outs = 0, at_tracks = 0;
+    };
+    std::vector<ChunkTabs> ct(chunks.size());
+    size_t max_tab = 0;
+    for (size_t ci = 0; ci < chunks.size(); ++ci) {
+      const Chunk& ch = chunks[ci];
+      ChunkTabs& T = ct[ci];
+      auto cpush = [&T](const void* p, size_t bytes) {
+        const size_t at = align256(T.tab.size());
+        T.tab.resize(at + bytes);
+        if (bytes) std::memcpy(T.tab.data() + at, p, bytes);
+        return at;
+      };
+      std::vector<FftOut> couts((size_t)(ch.end - ch.begin));
+      for (const Group& g : ch.groups) {
+        std::vector<FftSlot> slots(g.slots);
+        for (int i : g.jobs) {
+          const ear_conv_context& c = ctx[i];
+          const float* ra =
+              c.ir_next && c.dry_length > 0 ? (float*)((char*)ramps + at_ramp[i]) : nullptr;
+          slots[slot0[i]] = FftSlot{c.ir, c.dry, ra, c.ir ? c.ir_capacity : 0, c.ir_length,
+                                    c.dry_length};
+          if (c.ir_next)
+            slots[slot0[i] + 1] = FftSlot{c.ir_next, c.dry, ra ? ra + c.dry_length : nullptr,
+                                          c.ir_next_capacity, c.ir_next_length, c.dry_length};
+        }
+        std::vector<FftPair> pairs(g.pairs);
+        for (int p = 0; p < g.pairs; ++p) {
+          const int ia = g.jobs[2 * p];
+          const int ib = 2 * p + 1 < (int)g.jobs.size() ? g.jobs[2 * p + 1] : -1;
+          FftPair& P = pairs[p];
+          P.a0 = slot0[ia];
+          P.a1 = nslot[ia] == 2 ? slot0[ia] + 1 : -1;
+          P.b0 = ib >= 0 ? slot0[ib] : -1;
+          P.b1 = ib >= 0 && nslot[ib] == 2 ? slot0[ib] + 1 : -1;
+        }
+        T.at_slots.push_back(cpush(slots.data(), sizeof(FftSlot) * slots.size()));
+        T.at_pairs.push_back(cpush(pairs.data(), sizeof(FftPair) * pairs.size()));
+        // the inverse of each pair ends in A or B by the parity of the passes
+        float2* A = (float2*)(fft_arena + g.at_a);
+        float2* B = (float2*)(fft_arena + g.at_b);
+        const int npass = (g.log2l + 3) / 4;
+        float2* fwd = (npass % 2) ? B : A;
+        float2* prod = fwd == A ? B : A;
+        float2* inv = (npass % 2) ? (prod == A ? B : A) : prod;
+        const int64_t l = (int64_t)1 << g.log2l;
+        points += l * (int64_t)(g.slots + g.pairs);
+        for (int p = 0; p < g.pairs; ++p) {
+          for (int h = 0; h < 2 && 2 * p + h < (int)g.jobs.size(); ++h) {
+            const int i = g.jobs[2 * p + h];
+            const ear_conv_context& c = ctx[i];
+            couts[(size_t)(i - ch.begin)] =
+                FftOut{inv + (int64_t)p * l, c.offset,
+                       std::max(c.ir_length, c.ir_next ? c.ir_next_length : 0) + c.dry_length + 1,
+                       h};
+          }
         }
       }
-      std::vector<FftPair> pairs(g.pairs);
-      for (int p = 0; p < g.pairs; ++p) {
-        const int ia = g.jobs[2 * p];
-        const int ib = 2 * p + 1 < (int)g.jobs.size() ? g.jobs[2 * p + 1] : -1;
-        FftPair& P = pairs[p];
-        P.a0 = slot0[ia];
-        P.a1 = nslot[ia] == 2 ? slot0[ia] + 1 : -1;
-        P.b0 = ib >= 0 ? slot0[ib] : -1;
-        P.b1 = ib >= 0 && nslot[ib] == 2 ? slot0[ib] + 1 : -1;
+      T.at_outs = cpush(couts.data(), sizeof(FftOut) * couts.size());
+      std::vector<OutTrack> tr(tracks);
+      for (OutTrack& t : tr) {
+        const int b = std::max(t.begin, ch.begin), e = std::min(t.end, ch.end);
+        t.begin = b < e ? b - ch.begin : 0;
+        t.end = b < e ? e - ch.begin : 0;
       }
-      at_slots[gi] = push(slots.data(), sizeof(FftSlot) * slots.size());
-      at_pairs[gi] = push(pairs.data(), sizeof(FftPair) * pairs.size());
+      T.at_tracks = cpush(tr.data(), sizeof(OutTrack) * tr.size());
+      max_tab = std::max(max_tab, T.tab.size());
     }
-    const size_t at_outs_placeholder = push(couts.data(), sizeof(FftOut) * num);
-    const size_t at_tracks = push(tracks.data(), sizeof(OutTrack) * num_tracks);
-    CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
+    CU(ensure(&sc.tab, &sc.tab_cap, chunk_tab0 + max_tab));
     char* dtab = sc.tab;
     if (!fr.empty()) {
-      // copied with the rest below; launched after the copy
+      CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
+      k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, s>>>((const FadeRamp*)dtab, (int)fr.size());
+      ++launches;
     }
-    // run the groups; the inverse of each pair ends in buffer a or b
-    std::vector<float2*> pair_result(groups.size());
     auto passes = [&](float2* x, float2* y, int log2l, int count) -> float2* {
       // radix-16 passes, then one of radix 2/4/8 for the remaining bits
       int ns = 0;
@@ -1193,64 +1274,36 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
       }
       return in;  // holds the result
     };
-    // the output table needs the result buffers, known only after planning
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      Group& g = groups[gi];
-      float2* A = (float2*)(fft_arena + g.at_a);
-      float2* B = (float2*)(fft_arena + g.at_b);
-      const int lg = g.log2l;
-      const int npass = (lg + 3) / 4;
-      // forward: A -> ... ; product into the other buffer; inverse back
-      float2* fwd = (npass % 2) ? B : A;
-      float2* prod = fwd == A ? B : A;
-      const int ninv = npass;
-      float2* inv = (ninv % 2) ? (prod == A ? B : A) : prod;
-      pair_result[gi] = inv;
-      const int64_t l = (int64_t)1 << lg;
-      points += l * (int64_t)(g.slots + g.pairs);
-      for (int p = 0; p < g.pairs; ++p) {
-        const int ia = g.jobs[2 * p];
-        couts[ia] = FftOut{inv + (int64_t)p * l, ctx[ia].offset,
-                          std::max(ctx[ia].ir_length, ctx[ia].ir_next ? ctx[ia].ir_next_length : 0) +
-                              ctx[ia].dry_length + 1,
-                          0};
-        if (2 * p + 1 < (int)g.jobs.size()) {
-          const int ib = g.jobs[2 * p + 1];
-          couts[ib] = FftOut{inv + (int64_t)p * l, ctx[ib].offset,
-                            std::max(ctx[ib].ir_length, ctx[ib].ir_next ? ctx[ib].ir_next_length : 0) +
-                                ctx[ib].dry_length + 1,
-                            1};
-        }
+    for (size_t ci = 0; ci < chunks.size(); ++ci) {
+      const Chunk& ch = chunks[ci];
+      const ChunkTabs& T = ct[ci];
+      char* ctab = dtab + chunk_tab0;
+      // ordered after the previous chunk's kernels on the same stream
+      CU(cudaMemcpyAsync(ctab, T.tab.data(), T.tab.size(), cudaMemcpyHostToDevice, s));
+      for (size_t gi = 0; gi < ch.groups.size(); ++gi) {
+        const Group& g = ch.groups[gi];
+        float2* A = (float2*)(fft_arena + g.at_a);
+        float2* B = (float2*)(fft_arena + g.at_b);
+        const int lg = g.log2l;
+        const int64_t l = (int64_t)1 << lg;
+        dim3 gp((unsigned)((l + 255) / 256), (unsigned)g.slots);
+        k_fft_pack<<<gp, 256, 0, s>>>((const FftSlot*)(ctab + T.at_slots[gi]), A, lg);
+        ++launches;
+        float2* z = passes(A, B, lg, g.slots);
+        float2* w = z == A ? B : A;
+        dim3 gq((unsigned)((l + 255) / 256), (unsigned)g.pairs);
+        k_fft_product<<<gq, 256, 0, s>>>(z, (const FftPair*)(ctab + T.at_pairs[gi]), w, lg);
+        ++launches;
+        passes(w, z, lg, g.pairs);
       }
-    }
-    std::memcpy(tab.data() + at_outs_placeholder, couts.data(), sizeof(FftOut) * num);
-    CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
-    if (!fr.empty()) {
-      k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, s>>>((const FadeRamp*)(dtab + at_fr), (int)fr.size());
+      k_fft_accumulate<<<dim3((unsigned)((max_len + 255) / 256), (unsigned)num_tracks), 256, 0,
+                         s>>>((const FftOut*)(ctab + T.at_outs),
+                              (const OutTrack*)(ctab + T.at_tracks));
       ++launches;
+      CU(cudaGetLastError());
+      // the host tables are pageable: the copy above has been staged before
+      // cudaMemcpyAsync returned, so T may be reused
     }
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      Group& g = groups[gi];
-      float2* A = (float2*)(fft_arena + g.at_a);
-      float2* B = (float2*)(fft_arena + g.at_b);
-      const int lg = g.log2l;
-      const int64_t l = (int64_t)1 << lg;
-      dim3 gp((unsigned)((l + 255) / 256), (unsigned)g.slots);
-      k_fft_pack<<<gp, 256, 0, s>>>((const FftSlot*)(dtab + at_slots[gi]), A, lg);
-      ++launches;
-      float2* z = passes(A, B, lg, g.slots);
-      float2* w = z == A ? B : A;
-      dim3 gq((unsigned)((l + 255) / 256), (unsigned)g.pairs);
-      k_fft_product<<<gq, 256, 0, s>>>(z, (const FftPair*)(dtab + at_pairs[gi]), w, lg);
-      ++launches;
-      float2* v = passes(w, z, lg, g.pairs);
-      if (v != pair_result[gi])
-        return fail(EAR_ERR_STATE, "ear_convolve: internal buffer plan mismatch");
-    }
-    k_fft_accumulate<<<dim3((unsigned)((max_len + 255) / 256), (unsigned)num_tracks), 256, 0, s>>>(
-        (const FftOut*)(dtab + at_outs_placeholder), (const OutTrack*)(dtab + at_tracks));
-    ++launches;
-    CU(cudaGetLastError());
   }
   CU(cudaEventRecord(sc.ev[1], s));
   if (!on_dev)

@@ -274,3 +274,23 @@ def test_several_tracks_in_one_call_equal_separate_calls(mode):
     douts, _ = aural.convolve_tracks([dev(c) for c in flat], track_of, mode)
     for t in range(3):
         np.testing.assert_array_equal(bits(outs[t]), bits(douts[t].cpu().numpy()))
+
+
+def test_fft_in_memory_bounded_chunks_matches_one_pass(monkeypatch):
+    """With the transform scratch capped (EAR_FFT_CHUNK_BYTES) the contexts
+    run in several chunks; each chunk adds its contexts to the outputs in
+    order, so the result matches the one-pass call within the FFT tolerance
+    (pairs for the shared inverse transforms differ)."""
+    rng = np.random.default_rng(41)
+    per_track = [contexts_case("pairs", rng), contexts_case("offsets", rng)]
+    flat = per_track[0] + per_track[1]
+    track_of = [0] * len(per_track[0]) + [1] * len(per_track[1])
+    one, st1 = aural.convolve_tracks(flat, track_of, "fft")
+    monkeypatch.setenv("EAR_FFT_CHUNK_BYTES", str(1 << 20))  # about one context per chunk
+    many, st2 = aural.convolve_tracks(flat, track_of, "fft")
+    assert st2["launches"] > st1["launches"]
+    for a, b in zip(one, many):
+        assert np.abs(a - b).max() <= FFT_TOL * np.abs(a).max()
+    for t, p in enumerate(per_track):
+        ref, _ = oracle.convolve_fft64(p, len(many[t]))
+        assert np.abs(many[t] - ref).max() <= FFT_TOL * np.abs(ref).max()
