@@ -781,6 +781,392 @@ bool check_context(const ear_conv_context& c, int i) {
   return true;
 }
 
+
+// ---- ear_convolve_tracks, step by step
+
+// One call: contexts sorted by output track (each track's in the caller's
+// order), the tracks with their context ranges, statistics.
+struct ConvCall {
+  std::vector<ear_conv_context> ctx;
+  std::vector<OutTrack> tracks;
+  int64_t max_len = 0;
+  cudaStream_t s = nullptr;
+  Scratch* sc = nullptr;
+  int launches = 0;
+  double macs = 0;
+  int64_t points = 0;
+};
+
+void sort_by_track(const ear_conv_context* contexts, const int32_t* context_track, int num,
+                   float* const* outs, const int64_t* out_lengths, int num_tracks, ConvCall* c) {
+  std::vector<int> order(num);
+  for (int i = 0; i < num; ++i) order[i] = i;
+  if (context_track)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return context_track[x] < context_track[y]; });
+  c->ctx.resize(num);
+  c->tracks.resize(num_tracks);
+  for (int o = 0; o < num_tracks; ++o) {
+    c->tracks[o] = OutTrack{outs[o], out_lengths[o], 0, 0};
+    c->max_len = std::max(c->max_len, out_lengths[o]);
+  }
+  std::vector<char> seen(num_tracks, 0);
+  for (int k = 0; k < num; ++k) {
+    c->ctx[k] = contexts[order[k]];
+    const int o = context_track ? context_track[order[k]] : 0;
+    if (!seen[o]) {
+      c->tracks[o].begin = k;
+      seen[o] = 1;
+    }
+    c->tracks[o].end = k + 1;
+  }
+}
+
+// Response samples a context can read (the direct mode's joint range of a
+// keyframe pair; the FFT mode's [0, length)).
+int64_t ir_need(const ear_conv_context& c) {
+  return std::max(c.ir_length, c.ir_next ? c.ir_next_length : (int64_t)0);
+}
+
+// Host-memory calls: every distinct host buffer copied once into the arena
+// (a response serves as this keyframe's and the previous keyframe's
+// partner; a band serves every recorder), then the output tracks.
+struct Staging {
+  std::map<const float*, int64_t> spans;  // host buffer -> samples to copy
+  std::map<const float*, size_t> at;      // host buffer -> arena offset
+  std::vector<size_t> at_out;
+  size_t bytes = 0;
+};
+
+void plan_staging(const ConvCall& c, Staging* st) {
+  auto want = [st](const float* p, int64_t n) {
+    if (!p || n <= 0) return;
+    int64_t& v = st->spans[p];
+    v = std::max(v, n);
+  };
+  for (const ear_conv_context& x : c.ctx) {
+    want(x.ir, std::min(x.ir_capacity, ir_need(x)));
+    if (x.ir_next) want(x.ir_next, std::min(x.ir_next_capacity, ir_need(x)));
+    want(x.dry, x.dry_length);
+  }
+  for (const auto& kv : st->spans) {
+    st->at[kv.first] = st->bytes;
+    st->bytes += align256(sizeof(float) * (size_t)kv.second);
+  }
+  for (const OutTrack& t : c.tracks) {
+    st->at_out.push_back(st->bytes);
+    st->bytes += align256(sizeof(float) * (size_t)t.len);
+  }
+}
+
+// Copies the inputs and outputs and points the contexts and tracks at the
+// device copies.
+ear_status stage(ConvCall& c, const Staging& st, char* arena, float* const* outs) {
+  for (const auto& kv : st.spans)
+    CU(cudaMemcpyAsync(arena + st.at.at(kv.first), kv.first, sizeof(float) * kv.second,
+                       cudaMemcpyHostToDevice, c.s));
+  auto dev = [&](const float* p) {
+    return p && st.at.count(p) ? (const float*)(arena + st.at.at(p)) : nullptr;
+  };
+  for (ear_conv_context& x : c.ctx) {
+    const int64_t need = ir_need(x);
+    x.ir_capacity = x.ir ? std::min(x.ir_capacity, need) : 0;
+    x.ir = dev(x.ir);
+    if (x.ir_next) {
+      x.ir_next_capacity = std::min(x.ir_next_capacity, need);
+      x.ir_next = dev(x.ir_next);
+      if (!x.ir_next) {  // nothing to read: keep the context a keyframe pair
+        x.ir_next = x.ir ? x.ir : (const float*)arena;
+        x.ir_next_capacity = 0;
+      }
+    }
+    if (!x.ir) x.ir_capacity = 0;
+    x.dry = dev(x.dry);
+  }
+  for (size_t o = 0; o < c.tracks.size(); ++o) {
+    c.tracks[o].out = (float*)(arena + st.at_out[o]);
+    if (c.tracks[o].len > 0)
+      CU(cudaMemcpyAsync(c.tracks[o].out, outs[o], sizeof(float) * c.tracks[o].len,
+                         cudaMemcpyHostToDevice, c.s));
+  }
+  return EAR_OK;
+}
+
+// Appends 256-byte aligned blocks to a host table that is copied once.
+size_t push_block(std::vector<char>* tab, const void* p, size_t bytes) {
+  const size_t at = align256(tab->size());
+  tab->resize(at + bytes);
+  if (bytes) std::memcpy(tab->data() + at, p, bytes);
+  return at;
+}
+
+ear_status run_direct(ConvCall& c) {
+  const int num = (int)c.ctx.size();
+  std::vector<DirectCtx> dc(num);
+  bool any_interp = false;
+  for (int i = 0; i < num; ++i) {
+    const ear_conv_context& x = c.ctx[i];
+    DirectCtx& d = dc[i];
+    d.ir = x.ir;
+    d.ir2 = x.ir_next;
+    d.dry = x.dry;
+    d.cap = x.ir ? x.ir_capacity : 0;
+    d.cap2 = x.ir_next ? x.ir_next_capacity : 0;
+    d.first = x.ir_next ? std::min(x.ir_first, x.ir_next_first) : x.ir_first;
+    d.len = x.ir_next ? std::max(x.ir_length, x.ir_next_length) : x.ir_length;
+    d.n = x.dry_length;
+    d.off = x.offset;
+    d.inv_n = x.dry_length > 0 ? 1.0f / (float)(uint32_t)x.dry_length : 0.0f;
+    d.interp = x.ir_next ? 1 : 0;
+    any_interp |= d.interp != 0;
+    if (d.len > d.first && d.n > 0) c.macs += (double)d.n * (double)(d.len - d.first);
+  }
+  std::vector<char> tab;
+  const size_t at = push_block(&tab, dc.data(), sizeof(DirectCtx) * num);
+  const size_t at_t = push_block(&tab, c.tracks.data(), sizeof(OutTrack) * c.tracks.size());
+  Scratch& sc = *c.sc;
+  CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
+  CU(cudaMemcpyAsync(sc.tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, c.s));
+  const DirectCtx* d_ctx = (const DirectCtx*)(sc.tab + at);
+  const OutTrack* d_tracks = (const OutTrack*)(sc.tab + at_t);
+  const int tile = any_interp ? DirShape<true>::Tile : DirShape<false>::Tile;
+  const int64_t blocks = (c.max_len + tile - 1) / tile;
+  if (blocks > 0x7fffffffLL) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output too long");
+  const dim3 grid((unsigned)blocks, (unsigned)c.tracks.size());
+  if (any_interp)
+    k_conv_direct<true><<<grid, kDirThreads, 0, c.s>>>(d_ctx, d_tracks);
+  else
+    k_conv_direct<false><<<grid, kDirThreads, 0, c.s>>>(d_ctx, d_tracks);
+  ++c.launches;
+  CU(cudaGetLastError());
+  return EAR_OK;
+}
+
+// FFT mode plan: groups of equal transform size inside chunks of contexts
+// whose scratch fits fft_budget().  Each chunk adds its contexts to the
+// outputs in order, so the sums keep the order of one pass.
+struct Group {
+  int log2l;
+  std::vector<int> jobs;  // context indices in order
+  int slots = 0, pairs = 0;
+  size_t at_a = 0, at_b = 0;
+};
+
+struct Chunk {
+  int begin, end;
+  std::vector<Group> groups;
+  size_t bytes = 0;
+};
+
+struct FftPlan {
+  std::vector<Chunk> chunks;
+  std::vector<int> slot0, nslot, log2l_of;
+  std::vector<size_t> at_ramp;
+  size_t ramp_bytes = 0, fft_bytes = 0;
+};
+
+ear_status plan_fft(const ConvCall& c, FftPlan* p) {
+  const int num = (int)c.ctx.size();
+  p->slot0.assign(num, -1);
+  p->nslot.assign(num, 0);
+  p->log2l_of.assign(num, 0);
+  p->at_ramp.assign(num, 0);
+  for (int i = 0; i < num; ++i) {
+    const ear_conv_context& x = c.ctx[i];
+    int64_t mn = x.ir_length + x.dry_length + 1;
+    if (x.ir_next) mn = std::max(mn, x.ir_next_length + x.dry_length + 1);
+    p->log2l_of[i] = std::max(4, log2_ceil(mn));
+    if (p->log2l_of[i] > 30)
+      return fail(EAR_ERR_INVALID_ARG, "ear_convolve: a context needs a 2^%d transform",
+                  p->log2l_of[i]);
+    p->nslot[i] = x.ir_next ? 2 : 1;
+    if (x.ir_next && x.dry_length > 0) {
+      p->at_ramp[i] = p->ramp_bytes;
+      p->ramp_bytes += align256(sizeof(float) * 2 * (size_t)x.dry_length);
+    }
+  }
+  size_t run = 0;
+  const size_t budget = fft_budget();
+  for (int i = 0; i < num; ++i) {
+    // forward slots in A, pair results in B: about 2.5 transforms a slot
+    const size_t est = sizeof(float2) * ((size_t)5 * p->nslot[i] / 2 + 1) << p->log2l_of[i];
+    if (p->chunks.empty() || (run + est > budget && p->chunks.back().end > p->chunks.back().begin)) {
+      p->chunks.push_back(Chunk{i, i, {}, 0});
+      run = 0;
+    }
+    run += est;
+    p->chunks.back().end = i + 1;
+  }
+  for (Chunk& ch : p->chunks) {
+    for (int i = ch.begin; i < ch.end; ++i) {
+      auto it = std::find_if(ch.groups.begin(), ch.groups.end(),
+                             [&](const Group& g) { return g.log2l == p->log2l_of[i]; });
+      if (it == ch.groups.end()) {
+        ch.groups.push_back(Group{p->log2l_of[i], {}, 0, 0, 0, 0});
+        it = ch.groups.end() - 1;
+      }
+      it->jobs.push_back(i);
+    }
+    for (Group& g : ch.groups) {
+      for (int i : g.jobs) {
+        p->slot0[i] = g.slots;
+        g.slots += p->nslot[i];
+      }
+      g.pairs = ((int)g.jobs.size() + 1) / 2;
+      const size_t l = (size_t)1 << g.log2l;
+      g.at_a = ch.bytes;
+      ch.bytes += align256(sizeof(float2) * l * (size_t)g.slots);
+      g.at_b = ch.bytes;
+      ch.bytes += align256(sizeof(float2) * l * (size_t)std::max(g.slots, g.pairs));
+    }
+    p->fft_bytes = std::max(p->fft_bytes, ch.bytes);
+  }
+  return EAR_OK;
+}
+
+// Radix-16 passes, then one of radix 2/4/8 for the remaining bits; returns
+// the buffer that holds the result.
+float2* fft_passes(ConvCall& c, float2* x, float2* y, int log2l, int count) {
+  int ns = 0;
+  float2* in = x;
+  float2* o = y;
+  const int64_t l = (int64_t)1 << log2l;
+  while (ns < log2l) {
+    const int rem = log2l - ns;
+    const int lr = rem >= 4 ? 4 : rem;
+    const int64_t thr = l >> lr;
+    dim3 grid((unsigned)((thr + 255) / 256), (unsigned)count);
+    switch (lr) {
+      case 4: k_fft_pass<16><<<grid, 256, 0, c.s>>>(in, o, log2l, ns); break;
+      case 3: k_fft_pass<8><<<grid, 256, 0, c.s>>>(in, o, log2l, ns); break;
+      case 2: k_fft_pass<4><<<grid, 256, 0, c.s>>>(in, o, log2l, ns); break;
+      default: k_fft_pass<2><<<grid, 256, 0, c.s>>>(in, o, log2l, ns); break;
+    }
+    ++c.launches;
+    ns += lr;
+    std::swap(in, o);
+  }
+  return in;
+}
+
+ear_status run_fft(ConvCall& c, const FftPlan& p, char* fft_arena, float* ramps) {
+  const int num = (int)c.ctx.size();
+  // fade ramps of keyframe pairs (every chunk's), one table at the front
+  std::vector<char> tab;
+  std::vector<FadeRamp> fr;
+  for (int i = 0; i < num; ++i) {
+    const ear_conv_context& x = c.ctx[i];
+    if (!x.ir_next || x.dry_length <= 0) continue;
+    float* r = (float*)((char*)ramps + p.at_ramp[i]);
+    fr.push_back(FadeRamp{r, x.dry_length, 0});
+    fr.push_back(FadeRamp{r + x.dry_length, x.dry_length, 1});
+  }
+  if (!fr.empty()) push_block(&tab, fr.data(), sizeof(FadeRamp) * fr.size());
+  const size_t chunk_tab0 = align256(tab.size());
+  // per chunk: slot and pair tables of its groups, its contexts' results
+  // and the output tracks restricted to its contexts
+  struct ChunkTabs {
+    std::vector<char> tab;
+    std::vector<size_t> at_slots, at_pairs;
+    size_t at_outs = 0, at_tracks = 0;
+  };
+  std::vector<ChunkTabs> ct(p.chunks.size());
+  size_t max_tab = 0;
+  for (size_t ci = 0; ci < p.chunks.size(); ++ci) {
+    const Chunk& ch = p.chunks[ci];
+    ChunkTabs& T = ct[ci];
+    std::vector<FftOut> couts((size_t)(ch.end - ch.begin));
+    for (const Group& g : ch.groups) {
+      std::vector<FftSlot> slots(g.slots);
+      for (int i : g.jobs) {
+        const ear_conv_context& x = c.ctx[i];
+        const float* ra =
+            x.ir_next && x.dry_length > 0 ? (float*)((char*)ramps + p.at_ramp[i]) : nullptr;
+        slots[p.slot0[i]] = FftSlot{x.ir, x.dry, ra, x.ir ? x.ir_capacity : 0, x.ir_length,
+                                    x.dry_length};
+        if (x.ir_next)
+          slots[p.slot0[i] + 1] = FftSlot{x.ir_next, x.dry, ra ? ra + x.dry_length : nullptr,
+                                          x.ir_next_capacity, x.ir_next_length, x.dry_length};
+      }
+      std::vector<FftPair> pairs(g.pairs);
+      for (int q = 0; q < g.pairs; ++q) {
+        const int ia = g.jobs[2 * q];
+        const int ib = 2 * q + 1 < (int)g.jobs.size() ? g.jobs[2 * q + 1] : -1;
+        FftPair& P = pairs[q];
+        P.a0 = p.slot0[ia];
+        P.a1 = p.nslot[ia] == 2 ? p.slot0[ia] + 1 : -1;
+        P.b0 = ib >= 0 ? p.slot0[ib] : -1;
+        P.b1 = ib >= 0 && p.nslot[ib] == 2 ? p.slot0[ib] + 1 : -1;
+      }
+      T.at_slots.push_back(push_block(&T.tab, slots.data(), sizeof(FftSlot) * slots.size()));
+      T.at_pairs.push_back(push_block(&T.tab, pairs.data(), sizeof(FftPair) * pairs.size()));
+      // the inverse of each pair ends in A or B by the parity of the passes
+      float2* A = (float2*)(fft_arena + g.at_a);
+      float2* B = (float2*)(fft_arena + g.at_b);
+      const int npass = (g.log2l + 3) / 4;
+      float2* fwd = (npass % 2) ? B : A;
+      float2* prod = fwd == A ? B : A;
+      float2* inv = (npass % 2) ? (prod == A ? B : A) : prod;
+      const int64_t l = (int64_t)1 << g.log2l;
+      c.points += l * (int64_t)(g.slots + g.pairs);
+      for (int q = 0; q < g.pairs; ++q)
+        for (int h = 0; h < 2 && 2 * q + h < (int)g.jobs.size(); ++h) {
+          const int i = g.jobs[2 * q + h];
+          const ear_conv_context& x = c.ctx[i];
+          couts[(size_t)(i - ch.begin)] = FftOut{
+              inv + (int64_t)q * l, x.offset, ir_need(x) + x.dry_length + 1, h};
+        }
+    }
+    T.at_outs = push_block(&T.tab, couts.data(), sizeof(FftOut) * couts.size());
+    std::vector<OutTrack> tr(c.tracks);
+    for (OutTrack& t : tr) {
+      const int b = std::max(t.begin, ch.begin), e = std::min(t.end, ch.end);
+      t.begin = b < e ? b - ch.begin : 0;
+      t.end = b < e ? e - ch.begin : 0;
+    }
+    T.at_tracks = push_block(&T.tab, tr.data(), sizeof(OutTrack) * tr.size());
+    max_tab = std::max(max_tab, T.tab.size());
+  }
+  Scratch& sc = *c.sc;
+  CU(ensure(&sc.tab, &sc.tab_cap, chunk_tab0 + max_tab));
+  char* dtab = sc.tab;
+  if (!fr.empty()) {
+    CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, c.s));
+    k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, c.s>>>((const FadeRamp*)dtab, (int)fr.size());
+    ++c.launches;
+  }
+  for (size_t ci = 0; ci < p.chunks.size(); ++ci) {
+    const Chunk& ch = p.chunks[ci];
+    const ChunkTabs& T = ct[ci];
+    char* ctab = dtab + chunk_tab0;
+    // in stream order after the previous chunk's kernels; the pageable host
+    // table is staged before cudaMemcpyAsync returns
+    CU(cudaMemcpyAsync(ctab, T.tab.data(), T.tab.size(), cudaMemcpyHostToDevice, c.s));
+    for (size_t gi = 0; gi < ch.groups.size(); ++gi) {
+      const Group& g = ch.groups[gi];
+      float2* A = (float2*)(fft_arena + g.at_a);
+      float2* B = (float2*)(fft_arena + g.at_b);
+      const int lg = g.log2l;
+      const int64_t l = (int64_t)1 << lg;
+      dim3 gp((unsigned)((l + 255) / 256), (unsigned)g.slots);
+      k_fft_pack<<<gp, 256, 0, c.s>>>((const FftSlot*)(ctab + T.at_slots[gi]), A, lg);
+      ++c.launches;
+      float2* z = fft_passes(c, A, B, lg, g.slots);
+      float2* w = z == A ? B : A;
+      dim3 gq((unsigned)((l + 255) / 256), (unsigned)g.pairs);
+      k_fft_product<<<gq, 256, 0, c.s>>>(z, (const FftPair*)(ctab + T.at_pairs[gi]), w, lg);
+      ++c.launches;
+      fft_passes(c, w, z, lg, g.pairs);
+    }
+    k_fft_accumulate<<<dim3((unsigned)((c.max_len + 255) / 256), (unsigned)c.tracks.size()), 256,
+                       0, c.s>>>((const FftOut*)(ctab + T.at_outs),
+                                 (const OutTrack*)(ctab + T.at_tracks));
+    ++c.launches;
+    CU(cudaGetLastError());
+  }
+  return EAR_OK;
+}
+
 }  // namespace
 }  // namespace ear
 
@@ -939,388 +1325,59 @@ ear_status ear_convolve_tracks(const ear_conv_context* contexts, const int32_t* 
     if (!check_context(contexts[i], i)) return EAR_ERR_INVALID_ARG;
     if (context_track && (context_track[i] < 0 || context_track[i] >= num_tracks))
       return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d names track %d of %d", i,
-                  context_track ? context_track[i] : 0, num_tracks);
+                  context_track[i], num_tracks);
   }
-  int64_t max_len = 0;
-  for (int o = 0; o < num_tracks; ++o) max_len = std::max(max_len, out_lengths[o]);
-  if (num == 0 || max_len == 0) return EAR_OK;
+  ConvCall c;
+  sort_by_track(contexts, context_track, num, outs, out_lengths, num_tracks, &c);
+  if (num == 0 || c.max_len == 0) return EAR_OK;
+  FftPlan plan;
+  if (mode == EAR_CONV_FFT) {
+    const ear_status rc = plan_fft(c, &plan);
+    if (rc != EAR_OK) return rc;
+  }
   CU(cudaSetDevice(device));
   const bool on_dev = flags & EAR_AURAL_DEVICE_MEMORY;
-  cudaStream_t s = on_dev ? (cudaStream_t)stream : nullptr;
+  c.s = on_dev ? (cudaStream_t)stream : nullptr;
   Scratch& sc = scratch(device);
+  c.sc = &sc;
   std::lock_guard<std::mutex> lock(sc.mu);
   if (!sc.ev[0]) {
     CU(cudaEventCreate(&sc.ev[0]));
     CU(cudaEventCreate(&sc.ev[1]));
   }
-
-  // ---- stage the caller's buffers (host calls): one device arena, each
-  // distinct host buffer copied once (a response serves as this keyframe's
-  // and the previous keyframe's partner; a band serves every recorder)
-  // contexts grouped by output track, each track's in the caller's order
-  std::vector<int> order(num);
-  for (int i = 0; i < num; ++i) order[i] = i;
-  if (context_track)
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return context_track[x] < context_track[y]; });
-  std::vector<ear_conv_context> ctx(num);
-  std::vector<OutTrack> tracks(num_tracks);
-  for (int o = 0; o < num_tracks; ++o) tracks[o] = OutTrack{outs[o], out_lengths[o], 0, 0};
-  std::vector<char> seen(num_tracks, 0);
-  for (int k = 0; k < num; ++k) {
-    ctx[k] = contexts[order[k]];
-    const int o = context_track ? context_track[order[k]] : 0;
-    if (!seen[o]) {
-      tracks[o].begin = k;
-      seen[o] = 1;
-    }
-    tracks[o].end = k + 1;
-  }
-  size_t staged = 0;
-  auto ir_need = [](const ear_conv_context& c) {
-    return std::max(c.ir_length, c.ir_next ? c.ir_next_length : (int64_t)0);
-  };
-  std::map<const float*, int64_t> spans;  // host buffer -> samples to copy
-  std::map<const float*, size_t> at;      // host buffer -> arena offset
-  if (!on_dev) {
-    auto want = [&spans](const float* p, int64_t n) {
-      if (!p || n <= 0) return;
-      int64_t& v = spans[p];
-      v = std::max(v, n);
-    };
-    for (int i = 0; i < num; ++i) {
-      const ear_conv_context& c = ctx[i];
-      want(c.ir, std::min(c.ir_capacity, ir_need(c)));
-      if (c.ir_next) want(c.ir_next, std::min(c.ir_next_capacity, ir_need(c)));
-      want(c.dry, c.dry_length);
-    }
-    for (const auto& kv : spans) {
-      at[kv.first] = staged;
-      staged += align256(sizeof(float) * (size_t)kv.second);
-    }
-  }
-  std::vector<size_t> at_out(num_tracks, 0);
-  if (!on_dev) {
-    for (int o = 0; o < num_tracks; ++o) {
-      at_out[o] = staged;
-      staged += align256(sizeof(float) * (size_t)out_lengths[o]);
-    }
-  }
-
-  // ---- mode-specific scratch layout
-  struct Group {
-    int log2l;
-    std::vector<int> jobs;  // context indices in order
-    int slots = 0, pairs = 0;
-    size_t at_a = 0, at_b = 0;
-  };
-  // FFT scratch is bounded: contexts run in chunks (in their sorted order)
-  // whose transforms fit fft_budget(); each chunk adds its contexts to the
-  // outputs in order, so the sums keep the order of one pass
-  struct Chunk {
-    int begin, end;
-    std::vector<Group> groups;
-    size_t bytes = 0;
-  };
-  std::vector<Chunk> chunks;
-  std::vector<int> slot0(num, -1), nslot(num, 0), log2l_of(num, 0);
-  size_t fft_bytes = 0, ramp_bytes = 0;
-  std::vector<size_t> at_ramp(num, 0);
-  if (mode == EAR_CONV_FFT) {
-    for (int i = 0; i < num; ++i) {
-      const ear_conv_context& c = ctx[i];
-      int64_t mn = c.ir_length + c.dry_length + 1;
-      if (c.ir_next) mn = std::max(mn, c.ir_next_length + c.dry_length + 1);
-      log2l_of[i] = std::max(4, log2_ceil(mn));
-      if (log2l_of[i] > 30)
-        return fail(EAR_ERR_INVALID_ARG, "ear_convolve: context %d needs a 2^%d transform", i,
-                    log2l_of[i]);
-      nslot[i] = c.ir_next ? 2 : 1;
-      if (c.ir_next && c.dry_length > 0) {
-        at_ramp[i] = ramp_bytes;
-        ramp_bytes += align256(sizeof(float) * 2 * (size_t)c.dry_length);
-      }
-    }
-    size_t run = 0;
-    const size_t budget = fft_budget();
-    for (int i = 0; i < num; ++i) {
-      // forward slots in A, pair results in B: about 2.5 transforms a slot
-      const size_t est = sizeof(float2) * ((size_t)5 * nslot[i] / 2 + 1) << log2l_of[i];
-      if (chunks.empty() || (run + est > budget && chunks.back().end > chunks.back().begin)) {
-        chunks.push_back(Chunk{i, i, {}, 0});
-        run = 0;
-      }
-      run += est;
-      chunks.back().end = i + 1;
-    }
-    for (Chunk& ch : chunks) {
-      for (int i = ch.begin; i < ch.end; ++i) {
-        auto it = std::find_if(ch.groups.begin(), ch.groups.end(),
-                               [&](const Group& g) { return g.log2l == log2l_of[i]; });
-        if (it == ch.groups.end()) {
-          ch.groups.push_back(Group{log2l_of[i], {}, 0, 0, 0, 0});
-          it = ch.groups.end() - 1;
-        }
-        it->jobs.push_back(i);
-      }
-      for (Group& g : ch.groups) {
-        for (int i : g.jobs) {
-          slot0[i] = g.slots;
-          g.slots += nslot[i];
-        }
-        g.pairs = ((int)g.jobs.size() + 1) / 2;
-        const size_t l = (size_t)1 << g.log2l;
-        g.at_a = ch.bytes;
-        ch.bytes += align256(sizeof(float2) * l * (size_t)g.slots);
-        g.at_b = ch.bytes;
-        ch.bytes += align256(sizeof(float2) * l * (size_t)std::max(g.slots, g.pairs));
-      }
-      fft_bytes = std::max(fft_bytes, ch.bytes);
-    }
-  }
-  const size_t total_bytes = staged + ramp_bytes + fft_bytes;
+  // arena: staged inputs and outputs (host calls), fade ramps, transforms
+  Staging st;
+  if (!on_dev) plan_staging(c, &st);
+  const size_t total_bytes = st.bytes + plan.ramp_bytes + plan.fft_bytes;
   if (total_bytes > 0) CU(ensure(&sc.buf, &sc.cap, total_bytes));
   char* arena = sc.buf;
   if (!on_dev) {
-    for (const auto& kv : spans)
-      CU(cudaMemcpyAsync(arena + at[kv.first], kv.first, sizeof(float) * kv.second,
-                         cudaMemcpyHostToDevice, s));
-    auto dev = [&](const float* p) { return p && at.count(p) ? (const float*)(arena + at[p]) : nullptr; };
-    for (int i = 0; i < num; ++i) {
-      ear_conv_context& c = ctx[i];
-      c.ir_capacity = c.ir ? std::min(c.ir_capacity, ir_need(c)) : 0;
-      c.ir = dev(c.ir);
-      if (c.ir_next) {
-        c.ir_next_capacity = std::min(c.ir_next_capacity, ir_need(c));
-        c.ir_next = dev(c.ir_next);
-        if (!c.ir_next) {  // nothing to read: keep the context a keyframe pair
-          c.ir_next = c.ir ? c.ir : (const float*)arena;
-          c.ir_next_capacity = 0;
-        }
-      }
-      if (!c.ir) c.ir_capacity = 0;
-      c.dry = dev(c.dry);
-    }
-    for (int o = 0; o < num_tracks; ++o) {
-      tracks[o].out = (float*)(arena + at_out[o]);
-      if (out_lengths[o] > 0)
-        CU(cudaMemcpyAsync(tracks[o].out, outs[o], sizeof(float) * out_lengths[o],
-                           cudaMemcpyHostToDevice, s));
-    }
+    const ear_status rc = stage(c, st, arena, outs);
+    if (rc != EAR_OK) return rc;
   }
-  char* fft_arena = arena + staged + ramp_bytes;
-  float* ramps = (float*)(arena + staged);
-
-  // ---- small tables: one host block, one copy
-  std::vector<char> tab;
-  auto push = [&tab](const void* p, size_t bytes) {
-    const size_t at = align256(tab.size());
-    tab.resize(at + bytes);
-    if (bytes) std::memcpy(tab.data() + at, p, bytes);
-    return at;
-  };
-  int launches = 0;
-  double macs = 0;
-  int64_t points = 0;
-  CU(cudaEventRecord(sc.ev[0], s));
-  if (mode == EAR_CONV_DIRECT) {
-    std::vector<DirectCtx> dc(num);
-    bool any_interp = false;
-    for (int i = 0; i < num; ++i) {
-      const ear_conv_context& c = ctx[i];
-      DirectCtx& d = dc[i];
-      d.ir = c.ir;
-      d.ir2 = c.ir_next;
-      d.dry = c.dry;
-      d.cap = c.ir ? c.ir_capacity : 0;
-      d.cap2 = c.ir_next ? c.ir_next_capacity : 0;
-      d.first = c.ir_next ? std::min(c.ir_first, c.ir_next_first) : c.ir_first;
-      d.len = c.ir_next ? std::max(c.ir_length, c.ir_next_length) : c.ir_length;
-      d.n = c.dry_length;
-      d.off = c.offset;
-      d.inv_n = c.dry_length > 0 ? 1.0f / (float)(uint32_t)c.dry_length : 0.0f;
-      d.interp = c.ir_next ? 1 : 0;
-      any_interp |= d.interp != 0;
-      if (d.len > d.first && d.n > 0) macs += (double)d.n * (double)(d.len - d.first);
-    }
-    const size_t at = push(dc.data(), sizeof(DirectCtx) * num);
-    const size_t at_t = push(tracks.data(), sizeof(OutTrack) * num_tracks);
-    CU(ensure(&sc.tab, &sc.tab_cap, tab.size()));
-    CU(cudaMemcpyAsync(sc.tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
-    const DirectCtx* d_ctx = (const DirectCtx*)(sc.tab + at);
-    const OutTrack* d_tracks = (const OutTrack*)(sc.tab + at_t);
-    const int tile = any_interp ? DirShape<true>::Tile : DirShape<false>::Tile;
-    const int64_t blocks = (max_len + tile - 1) / tile;
-    if (blocks > 0x7fffffffLL) return fail(EAR_ERR_INVALID_ARG, "ear_convolve: output too long");
-    const dim3 grid((unsigned)blocks, (unsigned)num_tracks);
-    if (any_interp)
-      k_conv_direct<true><<<grid, kDirThreads, 0, s>>>(d_ctx, d_tracks);
-    else
-      k_conv_direct<false><<<grid, kDirThreads, 0, s>>>(d_ctx, d_tracks);
-    ++launches;
-    CU(cudaGetLastError());
-  } else {
-    // fade ramps of keyframe pairs (every chunk's), one table at the front
-    std::vector<FadeRamp> fr;
-    for (int i = 0; i < num; ++i) {
-      const ear_conv_context& c = ctx[i];
-      if (!c.ir_next || c.dry_length <= 0) continue;
-      float* r = (float*)((char*)ramps + at_ramp[i]);
-      fr.push_back(FadeRamp{r, c.dry_length, 0});
-      fr.push_back(FadeRamp{r + c.dry_length, c.dry_length, 1});
-    }
-    if (!fr.empty()) push(fr.data(), sizeof(FadeRamp) * fr.size());
-    const size_t chunk_tab0 = align256(tab.size());
-    // per chunk: slot and pair tables of its groups, its contexts' results
-    // and the output tracks restricted to its contexts
-    struct ChunkTabs {
-      std::vector<char> tab;
-      std::vector<size_t> at_slots, at_pairs;
-      size_t at_outs = 0, at_tracks = 0;
-    };
-    std::vector<ChunkTabs> ct(chunks.size());
-    size_t max_tab = 0;
-    for (size_t ci = 0; ci < chunks.size(); ++ci) {
-      const Chunk& ch = chunks[ci];
-      ChunkTabs& T = ct[ci];
-      auto cpush = [&T](const void* p, size_t bytes) {
-        const size_t at = align256(T.tab.size());
-        T.tab.resize(at + bytes);
-        if (bytes) std::memcpy(T.tab.data() + at, p, bytes);
-        return at;
-      };
-      std::vector<FftOut> couts((size_t)(ch.end - ch.begin));
-      for (const Group& g : ch.groups) {
-        std::vector<FftSlot> slots(g.slots);
-        for (int i : g.jobs) {
-          const ear_conv_context& c = ctx[i];
-          const float* ra =
-              c.ir_next && c.dry_length > 0 ? (float*)((char*)ramps + at_ramp[i]) : nullptr;
-          slots[slot0[i]] = FftSlot{c.ir, c.dry, ra, c.ir ? c.ir_capacity : 0, c.ir_length,
-                                    c.dry_length};
-          if (c.ir_next)
-            slots[slot0[i] + 1] = FftSlot{c.ir_next, c.dry, ra ? ra + c.dry_length : nullptr,
-                                          c.ir_next_capacity, c.ir_next_length, c.dry_length};
-        }
-        std::vector<FftPair> pairs(g.pairs);
-        for (int p = 0; p < g.pairs; ++p) {
-          const int ia = g.jobs[2 * p];
-          const int ib = 2 * p + 1 < (int)g.jobs.size() ? g.jobs[2 * p + 1] : -1;
-          FftPair& P = pairs[p];
-          P.a0 = slot0[ia];
-          P.a1 = nslot[ia] == 2 ? slot0[ia] + 1 : -1;
-          P.b0 = ib >= 0 ? slot0[ib] : -1;
-          P.b1 = ib >= 0 && nslot[ib] == 2 ? slot0[ib] + 1 : -1;
-        }
-        T.at_slots.push_back(cpush(slots.data(), sizeof(FftSlot) * slots.size()));
-        T.at_pairs.push_back(cpush(pairs.data(), sizeof(FftPair) * pairs.size()));
-        // the inverse of each pair ends in A or B by the parity of the passes
-        float2* A = (float2*)(fft_arena + g.at_a);
-        float2* B = (float2*)(fft_arena + g.at_b);
-        const int npass = (g.log2l + 3) / 4;
-        float2* fwd = (npass % 2) ? B : A;
-        float2* prod = fwd == A ? B : A;
-        float2* inv = (npass % 2) ? (prod == A ? B : A) : prod;
-        const int64_t l = (int64_t)1 << g.log2l;
-        points += l * (int64_t)(g.slots + g.pairs);
-        for (int p = 0; p < g.pairs; ++p) {
-          for (int h = 0; h < 2 && 2 * p + h < (int)g.jobs.size(); ++h) {
-            const int i = g.jobs[2 * p + h];
-            const ear_conv_context& c = ctx[i];
-            couts[(size_t)(i - ch.begin)] =
-                FftOut{inv + (int64_t)p * l, c.offset,
-                       std::max(c.ir_length, c.ir_next ? c.ir_next_length : 0) + c.dry_length + 1,
-                       h};
-          }
-        }
-      }
-      T.at_outs = cpush(couts.data(), sizeof(FftOut) * couts.size());
-      std::vector<OutTrack> tr(tracks);
-      for (OutTrack& t : tr) {
-        const int b = std::max(t.begin, ch.begin), e = std::min(t.end, ch.end);
-        t.begin = b < e ? b - ch.begin : 0;
-        t.end = b < e ? e - ch.begin : 0;
-      }
-      T.at_tracks = cpush(tr.data(), sizeof(OutTrack) * tr.size());
-      max_tab = std::max(max_tab, T.tab.size());
-    }
-    CU(ensure(&sc.tab, &sc.tab_cap, chunk_tab0 + max_tab));
-    char* dtab = sc.tab;
-    if (!fr.empty()) {
-      CU(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
-      k_fade_ramp<<<((int)fr.size() + 63) / 64, 64, 0, s>>>((const FadeRamp*)dtab, (int)fr.size());
-      ++launches;
-    }
-    auto passes = [&](float2* x, float2* y, int log2l, int count) -> float2* {
-      // radix-16 passes, then one of radix 2/4/8 for the remaining bits
-      int ns = 0;
-      float2* in = x;
-      float2* o = y;
-      const int64_t l = (int64_t)1 << log2l;
-      while (ns < log2l) {
-        const int rem = log2l - ns;
-        const int lr = rem >= 4 ? 4 : rem;
-        const int64_t thr = l >> lr;
-        dim3 grid((unsigned)((thr + 255) / 256), (unsigned)count);
-        switch (lr) {
-          case 4: k_fft_pass<16><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
-          case 3: k_fft_pass<8><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
-          case 2: k_fft_pass<4><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
-          default: k_fft_pass<2><<<grid, 256, 0, s>>>(in, o, log2l, ns); break;
-        }
-        ++launches;
-        ns += lr;
-        std::swap(in, o);
-      }
-      return in;  // holds the result
-    };
-    for (size_t ci = 0; ci < chunks.size(); ++ci) {
-      const Chunk& ch = chunks[ci];
-      const ChunkTabs& T = ct[ci];
-      char* ctab = dtab + chunk_tab0;
-      // ordered after the previous chunk's kernels on the same stream
-      CU(cudaMemcpyAsync(ctab, T.tab.data(), T.tab.size(), cudaMemcpyHostToDevice, s));
-      for (size_t gi = 0; gi < ch.groups.size(); ++gi) {
-        const Group& g = ch.groups[gi];
-        float2* A = (float2*)(fft_arena + g.at_a);
-        float2* B = (float2*)(fft_arena + g.at_b);
-        const int lg = g.log2l;
-        const int64_t l = (int64_t)1 << lg;
-        dim3 gp((unsigned)((l + 255) / 256), (unsigned)g.slots);
-        k_fft_pack<<<gp, 256, 0, s>>>((const FftSlot*)(ctab + T.at_slots[gi]), A, lg);
-        ++launches;
-        float2* z = passes(A, B, lg, g.slots);
-        float2* w = z == A ? B : A;
-        dim3 gq((unsigned)((l + 255) / 256), (unsigned)g.pairs);
-        k_fft_product<<<gq, 256, 0, s>>>(z, (const FftPair*)(ctab + T.at_pairs[gi]), w, lg);
-        ++launches;
-        passes(w, z, lg, g.pairs);
-      }
-      k_fft_accumulate<<<dim3((unsigned)((max_len + 255) / 256), (unsigned)num_tracks), 256, 0,
-                         s>>>((const FftOut*)(ctab + T.at_outs),
-                              (const OutTrack*)(ctab + T.at_tracks));
-      ++launches;
-      CU(cudaGetLastError());
-      // the host tables are pageable: the copy above has been staged before
-      // cudaMemcpyAsync returned, so T may be reused
-    }
-  }
-  CU(cudaEventRecord(sc.ev[1], s));
+  CU(cudaEventRecord(sc.ev[0], c.s));
+  const ear_status rc = mode == EAR_CONV_DIRECT
+                            ? run_direct(c)
+                            : run_fft(c, plan, arena + st.bytes + plan.ramp_bytes,
+                                      (float*)(arena + st.bytes));
+  if (rc != EAR_OK) return rc;
+  CU(cudaEventRecord(sc.ev[1], c.s));
   if (!on_dev)
     for (int o = 0; o < num_tracks; ++o)
       if (out_lengths[o] > 0)
-        CU(cudaMemcpyAsync(outs[o], tracks[o].out, sizeof(float) * out_lengths[o],
-                           cudaMemcpyDeviceToHost, s));
-  CU(cudaStreamSynchronize(s));
+        CU(cudaMemcpyAsync(outs[o], c.tracks[o].out, sizeof(float) * out_lengths[o],
+                           cudaMemcpyDeviceToHost, c.s));
+  CU(cudaStreamSynchronize(c.s));
   if (stats) {
     float ms = 0;
     cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]);
     stats->kernel_ms = ms;
-    stats->launches = launches;
-    stats->fft_points = points;
-    stats->multiply_adds = macs;
+    stats->launches = c.launches;
+    stats->fft_points = c.points;
+    stats->multiply_adds = c.macs;
   }
   return EAR_OK;
 }
+
 
 }  // extern "C"
