@@ -182,3 +182,26 @@ def test_cli_wav_writer_equals_reference_wavefile(tmp_path, norm, mx, stereo):
     rc, out = run_cli(*args)
     assert rc == 0, out
     assert (tmp_path / "got.wav").read_bytes() == (tmp_path / "ref.wav").read_bytes()
+
+
+def test_convolve_tracks_arguments_are_checked_before_device_work():
+    L = N.lib()
+    ctx = (N.EarConvContext * 2)()
+    track = np.array([0, 2], np.int32)  # track 2 of 2: out of range
+    a = np.zeros(8, np.float32)
+    b = np.zeros(8, np.float32)
+    outs = (C.c_void_p * 2)(a.ctypes.data, b.ctypes.data)
+    lens = (C.c_int64 * 2)(8, 8)
+    st = N.EarConvStats()
+    assert L.ear_convolve_tracks(ctx, track.ctypes.data, 2, 0, outs, lens, 2, 0, None, 0,
+                                 C.byref(st)) == N.EAR_ERR_INVALID_ARG
+    assert b"names track 2" in L.ear_last_error()
+    # several tracks need a track index per context
+    assert L.ear_convolve_tracks(ctx, None, 2, 0, outs, lens, 2, 0, None, 0,
+                                 C.byref(st)) == N.EAR_ERR_INVALID_ARG
+    # an output with samples but no buffer
+    bad = (C.c_void_p * 2)(a.ctypes.data, None)
+    track[1] = 1
+    assert L.ear_convolve_tracks(ctx, track.ctypes.data, 2, 0, bad, lens, 2, 0, None, 0,
+                                 C.byref(st)) == N.EAR_ERR_INVALID_ARG
+    assert b"output track 1" in L.ear_last_error()
