@@ -638,9 +638,15 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(w, args.cpu_rays or _default_cpu_rays(args.workload), os.cpu_count() or 1)
+        sample = args.cpu_rays or _default_cpu_rays(args.workload)
+        cpu = cpu_baseline(w, sample, os.cpu_count() or 1)
         cpu.pop("seconds", None)
         cpu.pop("segments", None)
+        # the reference's own threading: one thread per (source, keyframe,
+        # band) context (src/EAR.cpp:193-207), i.e. 3 for one context
+        ref3 = cpu_baseline(w, max(1, sample // 4), 3)
+        cpu["reference_threading"] = {"value": ref3["value"], "unit": "segments/s",
+                                      "threads": 3, "sample_rays_per_band": max(1, sample // 4)}
 
     if rank == 0:
         cfg = _config(w, args, flush="flushed before every step (512 MB write)")
