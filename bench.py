@@ -652,6 +652,8 @@ def run_ours(args):
         cfg = _config(w, args, flush="flushed before every step (512 MB write)")
         cfg["mode"] = "exact (--fmad=false)" if exact else "fast"
         cfg["bvh"] = tracer.info()
+        # tree quality beside segments/s (unit node and triangle costs)
+        cfg["bvh"]["sah_cost"] = {"binary": tracer.sah_cost(2), "wide4": tracer.sah_cost(4)}
         cfg["rays_per_s"] = agg["rays"] / (total_ms / 1000.0) * world
         line = {
             "metric": "ray-bounce segments/s", "value": value, "unit": "segments/s",

@@ -329,6 +329,71 @@ ear_status ear_scene_info(const ear_scene* s, int64_t* num_triangles, int64_t* n
   return EAR_OK;
 }
 
+ear_status ear_scene_sah_cost(const ear_scene* s, int32_t width, float node_cost,
+                              float triangle_cost, double* cost) {
+  if (!s || !cost || (width != 2 && width != 4))
+    return fail(EAR_ERR_INVALID_ARG, "ear_scene_sah_cost: bad arguments");
+  if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_sah_cost before ear_scene_build_bvh");
+  CU(cudaSetDevice(s->device));
+  auto area = [](float lx, float hx, float ly, float hy, float lz, float hz) {
+    const double dx = std::max(0.0, (double)hx - lx), dy = std::max(0.0, (double)hy - ly),
+                 dz = std::max(0.0, (double)hz - lz);
+    return 2.0 * (dx * dy + dy * dz + dz * dx);
+  };
+  auto leaf_count = [](int child) { return (((uint32_t)~child) >> kLeafCountShift) + 1; };
+  // every node is entered through its parent's box: internal children cost
+  // node_cost, leaves triangle_cost per triangle, each weighted by the box
+  // area over the root's
+  double sum = 0.0, root = 0.0;
+  if (width == 2) {
+    std::vector<Node> n((size_t)s->ds.num_nodes);
+    CU(cudaMemcpy(n.data(), s->ds.nodes, sizeof(Node) * n.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n.size(); ++i) {
+      const Node& q = n[i];
+      const double a0 = area(q.a.x, q.a.y, q.a.z, q.a.w, q.b.x, q.b.y);
+      const double a1 = area(q.b.z, q.b.w, q.c.x, q.c.y, q.c.z, q.c.w);
+      const int ch[2] = {q.d.x, q.d.y};
+      const double ar[2] = {a0, a1};
+      for (int j = 0; j < 2; ++j)
+        sum += ch[j] >= 0 ? node_cost * ar[j] : triangle_cost * leaf_count(ch[j]) * ar[j];
+      if (i == 0) {
+        root = area(std::min(q.a.x, q.b.z), std::max(q.a.y, q.b.w), std::min(q.a.z, q.c.x),
+                    std::max(q.a.w, q.c.y), std::min(q.b.x, q.c.z), std::max(q.b.y, q.c.w));
+      }
+    }
+  } else {
+    if (!s->ds.nodes4) return fail(EAR_ERR_STATE, "the scene has no 4-wide tree");
+    std::vector<Node4> n((size_t)s->ds.num_nodes4);
+    CU(cudaMemcpy(n.data(), s->ds.nodes4, sizeof(Node4) * n.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n.size(); ++i) {
+      const Node4& q = n[i];
+      const float* lx = &q.lox.x;
+      const float* hx = &q.hix.x;
+      const float* ly = &q.loy.x;
+      const float* hy = &q.hiy.x;
+      const float* lz = &q.loz.x;
+      const float* hz = &q.hiz.x;
+      const int* ch = &q.child.x;
+      float u[6] = {1e30f, -1e30f, 1e30f, -1e30f, 1e30f, -1e30f};
+      for (int j = 0; j < 4; ++j) {
+        if (!((q.meta.y >> j) & 1)) continue;
+        const double a = area(lx[j], hx[j], ly[j], hy[j], lz[j], hz[j]);
+        sum += ch[j] >= 0 ? node_cost * a : triangle_cost * leaf_count(ch[j]) * a;
+        u[0] = std::min(u[0], lx[j]);
+        u[1] = std::max(u[1], hx[j]);
+        u[2] = std::min(u[2], ly[j]);
+        u[3] = std::max(u[3], hy[j]);
+        u[4] = std::min(u[4], lz[j]);
+        u[5] = std::max(u[5], hz[j]);
+      }
+      if (i == 0) root = area(u[0], u[1], u[2], u[3], u[4], u[5]);
+    }
+  }
+  // the root node itself is always entered
+  *cost = root > 0 ? node_cost + sum / root : 0.0;
+  return EAR_OK;
+}
+
 void ear_scene_destroy(ear_scene* s) {
   if (!s) return;
   cudaSetDevice(s->device);

@@ -204,6 +204,14 @@ class Tracer:
                 "builder": getattr(self, "_builder", "default"),
                 "width": getattr(self, "_width", 2)}
 
+    def sah_cost(self, width: int = 4, node_cost: float = 1.0,
+                 triangle_cost: float = 1.0) -> float:
+        """Surface-area-heuristic cost of the binary (2) or 4-wide (4) tree."""
+        c = C.c_double()
+        N.check(N.lib().ear_scene_sah_cost(self._h, int(width), float(node_cost),
+                                           float(triangle_cost), C.byref(c)))
+        return c.value
+
     def set_width(self, width: int) -> None:
         """Traverse the binary (2) or 4-wide (4) tree; no rebuild."""
         N.check(N.lib().ear_scene_set_bvh_width(self._h, int(width)))

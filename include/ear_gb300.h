@@ -220,6 +220,14 @@ ear_status ear_scene_build_bvh(ear_scene* scene, const ear_bvh_opts* opts);
 ear_status ear_scene_info(const ear_scene* scene, int64_t* num_triangles,
                           int64_t* num_nodes, int32_t* max_depth,
                           float* box_pad, int64_t* device_bytes);
+
+/* Surface-area-heuristic cost of the built tree (width 2: binary, 4:
+   4-wide): node_cost per entered internal node plus triangle_cost per
+   triangle of an entered leaf, each weighted by its box area over the
+   root's, plus the root.  A tree-quality figure to read beside segments/s:
+   a worse tree inflates the node and triangle fetches per segment. */
+ear_status ear_scene_sah_cost(const ear_scene* scene, int32_t width, float node_cost,
+                              float triangle_cost, double* cost);
 void ear_scene_destroy(ear_scene* scene);
 
 /* Number of tracks the recorders produce (1 per mono, 2 per stereo). */

@@ -108,6 +108,11 @@ def test_track_functions_match_oracle():
         oracle.lib().oracle_track_t60(b.ctypes.data, first, last)
 
 
+def test_sah_cost_arguments_are_checked_before_device_work():
+    c = C.c_double()
+    assert N.lib().ear_scene_sah_cost(None, 4, 1.0, 1.0, C.byref(c)) == N.EAR_ERR_INVALID_ARG
+
+
 def test_batch_arguments_are_checked_before_device_work():
     h = C.c_void_p()
     p = N.EarRenderParams()

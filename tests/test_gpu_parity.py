@@ -227,3 +227,17 @@ def test_split_by_ray_range_equals_whole_render():
     assert (np.abs(e1 - e2) <= 1e-5 * np.maximum(e2, 1e-30)).all()
     assert (np.minimum(parts[0].first_sample, parts[1].first_sample) == whole.first_sample).all()
     assert (np.maximum(parts[0].last_sample, parts[1].last_sample) == whole.last_sample).all()
+
+
+def test_sah_cost_ranks_the_builders():
+    """ear_scene_sah_cost: positive and finite for both trees; the PLOC
+    binary tree (locally ordered clustering) costs less than the LBVH's
+    (Morton splits), as the builders' measured traversal speeds order them."""
+    w = scenes.relief_hall()
+    costs = {}
+    for builder in ("lbvh", "ploc"):
+        with _tracer(w, builder=builder, width=0) as tr:
+            costs[builder] = (tr.sah_cost(2), tr.sah_cost(4))
+    for b2, b4 in costs.values():
+        assert np.isfinite(b2) and np.isfinite(b4) and b2 > 1.0 and b4 > 1.0
+    assert costs["ploc"][0] < costs["lbvh"][0]
