@@ -54,7 +54,8 @@ def encode(*, materials, meshes, sources, recorders, settings: Optional[dict] = 
            keys: Optional[Sequence[float]] = None, freq=(0.3, 2.0, 6.0)) -> bytes:
     """materials: [(name, refl3, refr3|None, spec3|None)];
     meshes: [(material name, (n, 9) triangles)];
-    sources: [dict(file=..., location=(3,)|(K,3), gain=..., offset=...)];
+    sources: [dict(file=... | files=[low, mid, high], location=(3,)|(K,3), gain=...,
+    offset=...)] (three files: a 3SRC block);
     recorders: [dict(file=..., location=..., channels=1|2, right_ear=...,
     head_size=..., head_absorption=(3,))]."""
     out = [b".EAR", _block("VRSN", [0])]
@@ -79,10 +80,13 @@ def encode(*, materials, meshes, sources, recorders, settings: Optional[dict] = 
         t = np.asarray(tris, np.float32).reshape(-1, 3, 3)
         out.append(_block("MESH", [mat] + [[list(map(float, v)) for v in tri] for tri in t]))
     for s in sources:
-        items = [s.get("file", "dry.wav"), _loc(s["location"]), float(s.get("gain", 1.0))]
+        files = s.get("files")
+        triple = files is not None and len(files) == 3  # 3SRC: one WAV per band
+        names = list(files) if triple else [s.get("file", files[0] if files else "dry.wav")]
+        items = names + [_loc(s["location"]), float(s.get("gain", 1.0))]
         if "offset" in s:
             items.append(float(s["offset"]))
-        out.append(_block("SSRC", items))
+        out.append(_block("3SRC" if triple else "SSRC", items))
     for r in recorders:
         ch = int(r.get("channels", 1))
         items = [r.get("file", "out.wav"), 35.0, _loc(r["location"])]

@@ -119,18 +119,23 @@ def test_presets_room_exact_parity():
     assert (np.abs(e1 - e2) <= 1e-5 * np.maximum(e2, 1e-300)).all()
 
 
-def keyed_scene(tmp_path):
+def keyed_scene(tmp_path, triple=False):
     """The presets room with two keyframes: the source moves, the recorders
-    stay; a 0.4 s dry sound."""
+    stay; a 0.4 s dry sound (or, triple, three 0.4 s band WAVs: a 3SRC)."""
     sc = earfile.read_ear(GOLDEN / "presets_room.ear")
     loc = np.asarray(sc.sources[0]["location"], np.float32)
     src = {"file": "dry.wav", "location": np.stack([loc, loc + np.float32([0.8, 0.2, 0.0])]),
            "gain": 1.0}
+    if triple:
+        src["files"] = ["b0.wav", "b1.wav", "b2.wav"]
     recs = [dict(r) for r in sc.recorders]
     settings = dict(sc.settings, samples=20000)
     blob = earfile.encode(materials=sc.materials, meshes=sc.meshes, sources=[src], recorders=recs,
                           settings=settings, keys=[0.0, 0.2], freq=sc.freq)
     (tmp_path / "keyed.ear").write_bytes(blob)
+    if triple:
+        return sc, [write_dry(tmp_path / f"b{b}.wav", 0.3 + 0.05 * b, seed=10 + b)
+                    for b in range(3)]
     return sc, write_dry(tmp_path / "dry.wav", 0.4, seed=4)
 
 
@@ -141,7 +146,8 @@ def reconstruct(tmp_path, sc, dry, mode):
     from ear_gb300.aural import Context, Track, section
 
     keys = [np.float32(0.0), np.float32(0.2)]
-    bands = oracle.band_split(dry, sc.freq)
+    # 3SRC: the three WAVs are the bands (TripleBandSoundFile::Band)
+    bands = dry if isinstance(dry, list) else oracle.band_split(dry, sc.freq)
     ctx = []
     for kf in range(2):
         stem = tmp_path / "dump" / f"context-0-{kf}"
@@ -218,3 +224,18 @@ def test_render_auralises_keyframes_fft(tmp_path):
         got, _ = read_wav16(tmp_path / name)
         assert got.shape == pcm.shape, name
         assert np.abs(got.astype(np.int32) - pcm.astype(np.int32)).max() <= 1, name
+
+
+def test_render_auralises_a_triple_band_source_bit_exact(tmp_path):
+    """A 3SRC source (one WAV per band, no equalizer; bands of unequal
+    length) auralised with --conv direct equals the restatement."""
+    sc, bands = keyed_scene(tmp_path, triple=True)
+    r = subprocess.run([str(CLI), "render", "keyed.ear", "--seed", "5", "--exact", "--seconds", "1",
+                        "--conv", "direct", "--dump-tracks", "dump"],
+                       capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout
+    ref = reconstruct(tmp_path, sc, bands, "direct")
+    for name, pcm in ref.items():
+        got, _ = read_wav16(tmp_path / name)
+        assert got.shape == pcm.shape, name
+        np.testing.assert_array_equal(got, pcm)
