@@ -239,3 +239,35 @@ def test_render_auralises_a_triple_band_source_bit_exact(tmp_path):
         got, _ = read_wav16(tmp_path / name)
         assert got.shape == pcm.shape, name
         np.testing.assert_array_equal(got, pcm)
+
+
+def test_render_debugdir_writes_the_references_debug_files(tmp_path):
+    """With the 'debugdir' setting the CLI writes the reference's debug
+    files (src/EAR.cpp:122-146, 229-240, 362-372): the equalizer bands, the
+    impulse responses (.wav, .bin) and each context's processed recorder,
+    normalised as Recorder::Save(fn) does (mono: peak 0.8 of full scale)."""
+    sc = earfile.read_ear(GOLDEN / "presets_room.ear")
+    loc = np.asarray(sc.sources[0]["location"], np.float32)
+    src = {"file": "dry.wav", "location": np.stack([loc, loc + np.float32([0.5, 0.0, 0.0])])}
+    settings = dict(sc.settings, samples=20000, debugdir="dbg")
+    blob = earfile.encode(materials=sc.materials, meshes=sc.meshes, sources=[src],
+                          recorders=[dict(r) for r in sc.recorders], settings=settings,
+                          keys=[0.0, 0.2], freq=sc.freq)
+    (tmp_path / "dbg.ear").write_bytes(blob)
+    write_dry(tmp_path / "dry.wav", 0.4, seed=2)
+    r = subprocess.run([str(CLI), "render", "dbg.ear", "--seed", "2", "--seconds", "1"],
+                       capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout
+    d = tmp_path / "dbg"
+    names = {p.name for p in d.iterdir()}
+    lomihi = ["low", "mid", "high"]
+    for b in range(3):
+        assert f"sound-0.band-{b}{lomihi[b]}.wav" in names
+        for kf in range(2):
+            for ri in range(2):
+                assert f"response-{ri}.sound-0.frame-{kf:02d}.band-{b}{lomihi[b]}.wav" in names
+                assert f"response-{ri}.sound-0.frame-{kf:02d}.band-{b}{lomihi[b]}.bin" in names
+                assert f"rec-{ri}.sound-0.frame-{kf:02d}.band-{b}.wav" in names
+    pcm, _ = read_wav16(d / "rec-0.sound-0.frame-00.band-1.wav")
+    assert pcm.shape[1] == 1
+    assert abs(int(np.abs(pcm.astype(np.int64)).max()) - 0.8 * 32768) <= 2
