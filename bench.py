@@ -461,7 +461,7 @@ def auralisation(device: int, steps: int, cpu: bool):
                                "note": "45 transforms of 8 MB: partly L2-resident"}}
     dir_ms, _ = timed(lambda: run("direct"), 1)
     ks, st = kstat["direct"]
-    macs = float(st["multiply_adds"]) * tracks
+    macs = float(st["multiply_adds"])  # all 30 contexts of the one call
     # FP32 without contraction: a multiply and an add per term, 128 lanes x
     # 152 SMs at the sampled clock
     res["direct"] = {"ms": dir_ms, "kernel_ms": ks, "terms": macs,
