@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
 the CPU-baseline legs of bench.py, as the checker or the timed baseline.
-The product (ear_gb300) never imports this package.  PARITY UNPINNED: see
-the header of ear_oracle.cpp.
+The product (ear_gb300) never imports this package.  PARITY UNPINNED for
+the ray-tracing path (see the header of ear_oracle.cpp); the band split is
+pinned to the reference's own equalizer (oracle/_ref).
 """
 from __future__ import annotations
 

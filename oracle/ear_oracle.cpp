@@ -24,6 +24,10 @@
 //      powf() instead, for the statistical comparison.
 // Everything else (FloatBuffer bookkeeping, the 1/N and gain^2 scaling
 // quirks, the float-accumulated ray count) follows the reference verbatim.
+// The auralisation restatement at the end of this file (equalizer band
+// split, RecorderTrack::Process) is pinned: the band split equals the
+// reference's own lib/equalizer/Equalizer.cpp bit for bit, compiled into
+// oracle/_ref by oracle/build_ref.py where the reference tree exists.
 // Compile with -ffp-contract=off: the restatement relies on IEEE single
 // precision with no fused multiply-adds.
 
