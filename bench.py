@@ -543,7 +543,7 @@ def run_ours(args):
     kw["first_ray"] = rank * int(kw["num_rays"])
     exact = args.exact
     tracer = Tracer(w.vertices, w.material_ids, w.materials, device=local, box_pad=args.box_pad,
-                    builder=args.builder, width=args.width)
+                    builder=args.builder, width=args.width, visibility_map=args.vismap)
     tracks = w.num_tracks
     out = torch.zeros((tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -552,8 +552,9 @@ def run_ours(args):
     def step():
         return tracer.render(w.source, w.recorders, out=out, exact=exact, **kw)
 
+    map_build_ms = 0.0
     for _ in range(max(3, args.warmup)):
-        step()
+        map_build_ms += float(step().stats["map_build_ms"])
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
@@ -563,7 +564,7 @@ def run_ours(args):
     kern_ms = 0.0
     seg = 0
     agg = {"node_visits": 0, "triangle_tests": 0, "splat_bins": 0, "segments": 0, "rays": 0,
-           "shadow_queries": 0}
+           "shadow_queries": 0, "map_entries": 0}
     launches = 0
     t_wall = time.perf_counter()
     for _ in range(args.steps):
@@ -590,7 +591,7 @@ def run_ours(args):
 
     # roofline of the trace kernel: algorithmic bytes / kernel time
     alg_bytes = 64.0 * agg["node_visits"] + 48.0 * agg["triangle_tests"] + 64.0 * agg["segments"] \
-        + 4.0 * agg["splat_bins"]
+        + 4.0 * agg["splat_bins"] + 8.0 * agg["map_entries"]
     achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else 0.0
     hbm, src = peaks()
     per_launch = alg_bytes / args.steps
@@ -616,7 +617,7 @@ def run_ours(args):
         e0.record(stream)
         for _ in range(e_steps):
             t2 = Tracer(vp, mp, w.materials, device=local, box_pad=args.box_pad,
-                        builder=args.builder, width=args.width)
+                        builder=args.builder, width=args.width, visibility_map=args.vismap)
             r2 = t2.render(w.source, w.recorders, out=host_out, exact=exact, **kw)
             t2.close()
             e_seg += int(r2.stats["segments"])
@@ -661,6 +662,15 @@ def run_ours(args):
         cfg["bvh"] = tracer.info()
         # tree quality beside segments/s (unit node and triangle costs)
         cfg["bvh"]["sah_cost"] = {"binary": tracer.sah_cost(2), "wide4": tracer.sah_cost(4)}
+        # listener visibility maps (built during warm-up, reused by the
+        # timed steps like the tree; e2e builds them inside every step)
+        cfg["visibility_map"] = {"setting": args.vismap, "build_ms": map_build_ms,
+                                 "cells_per_face_edge": int(res.stats["map_res"]),
+                                 "bytes": int(res.stats["map_bytes"]),
+                                 "entries_read_per_segment":
+                                     agg["map_entries"] / max(1, agg["segments"]),
+                                 "shadow_queries_per_segment":
+                                     agg["shadow_queries"] / max(1, agg["segments"])}
         cfg["rays_per_s"] = agg["rays"] / (total_ms / 1000.0) * world
         line = {
             "metric": "ray-bounce segments/s", "value": value, "unit": "segments/s",
@@ -701,6 +711,8 @@ def main():
     ap.add_argument("--builder", default="default", choices=["default", "lbvh", "ploc"])
     ap.add_argument("--width", type=int, default=0, choices=[0, 2, 4],
                     help="BVH traversal width (0: by scene size)")
+    ap.add_argument("--vismap", type=int, default=0,
+                    help="listener visibility maps: 0 automatic, -1 off, 8..2048 cells per face edge")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

@@ -49,7 +49,7 @@ class EarSceneDesc(C.Structure):
 class EarBvhOpts(C.Structure):
     _fields_ = [("box_pad", C.c_float), ("max_leaf_size", C.c_int32), ("builder", C.c_int32),
                 ("ploc_radius", C.c_int32), ("width", C.c_int32), ("visibility_order", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("visibility_map", C.c_int32), ("reserved", C.c_int32)]
 
 
 class EarRecorder(C.Structure):
@@ -74,7 +74,9 @@ class EarRenderStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("segments", C.c_uint64), ("shadow_queries", C.c_uint64),
                 ("contributions", C.c_uint64), ("sampler_overflows", C.c_uint64),
                 ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64),
-                ("splat_bins", C.c_uint64), ("kernel_ms", C.c_double)]
+                ("splat_bins", C.c_uint64), ("kernel_ms", C.c_double),
+                ("map_entries", C.c_uint64), ("map_build_ms", C.c_double),
+                ("map_bytes", C.c_uint64), ("map_res", C.c_int32), ("reserved1", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -43,6 +43,7 @@ CUDA_UNITS = [
     ("trace_fast.cu", ["--fmad=true"]),
     ("api.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
+    ("vismap.cu", ["--fmad=false"]),
     # exact paths use explicit _rn intrinsics; the FFT may contract
     ("aural.cu", ["--fmad=true"]),
 ]

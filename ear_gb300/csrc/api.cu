@@ -45,6 +45,8 @@ thread_local char g_err[512] = "";
 // (measured +4..6% segments/s over the LBVH on the 20,000- and
 // 2,000,000-triangle scenes).
 constexpr int kDefaultBuilder = EAR_BVH_PLOC;
+// Visibility-map cells with more entries than this are left to the tree.
+constexpr int kVisWalkCap = 96;
 
 ear_status fail(ear_status st, const char* fmt, ...) {
   va_list ap;
@@ -114,6 +116,8 @@ void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel
   stats->triangle_tests = cnt[kTriTests];
   stats->splat_bins = cnt[kSplatBins];
   stats->kernel_ms = kernel_ms;
+  stats->map_entries = cnt[kMapEntries];
+  stats->map_build_ms = 0.0;
 }
 
 namespace fin {
@@ -298,6 +302,12 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   s->ds.any_order = order;
   s->ds.any_far = order == 2 ? 1 : 0;
   s->probe_valid = false;
+  const int vmap = opts ? opts->visibility_map : 0;
+  if (vmap < -1 || (vmap > 0 && (vmap < 8 || vmap > 2048)))
+    return fail(EAR_ERR_INVALID_ARG, "visibility_map must be -1, 0 or 8..2048");
+  s->vis_opt = vmap;
+  free_vis_map(&s->vis);
+  s->vis_valid = false;
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
@@ -411,6 +421,7 @@ void ear_scene_destroy(ear_scene* s) {
   cudaFree(s->recs);
   cudaFree(s->emitter);
   cudaFree(s->probe);
+  free_vis_map(&s->vis);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   delete s;
@@ -455,6 +466,78 @@ ear_status choose_visibility_order(ear_scene* s, const ear_recorder* recs, int32
   }
   a.any_far = s->ds.any_far;
   return EAR_OK;
+}
+
+// Listener visibility maps for the recorder set (ear_bvh_opts.
+// visibility_map): built on first use, reused while the set, the tree and
+// the setting stay the same.  A set whose lists would exceed the entry
+// limit keeps the tree traversal.  *build_ms receives the build time.
+ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t nrec, TraceArgs& a,
+                               cudaStream_t st, double* build_ms) {
+  *build_ms = 0.0;
+  a.vis_res = 0;
+  if (nrec <= 0 || s->vis_opt < 0 || s->ds.num_tris <= 0) return EAR_OK;
+  const bool automatic = s->vis_opt == 0;
+  int res = s->vis_opt;
+  if (automatic) {
+    const double r = 4.0 * std::sqrt((double)s->ds.num_tris);
+    res = (int)std::min(2048.0, std::max(64.0, std::floor(r / 64.0) * 64.0));
+  }
+  uint64_t key = 1469598103934665603ull ^ (uint64_t)res;
+  for (int32_t i = 0; i < nrec; ++i)
+    for (int k = 0; k < 3; ++k) {
+      uint32_t bits;
+      std::memcpy(&bits, &recs[i].location[k], sizeof bits);
+      key = (key ^ bits) * 1099511628211ull;
+    }
+  key = (key ^ (uint64_t)nrec) * 1099511628211ull;
+  if (!s->vis_valid || key != s->vis_key) {
+    free_vis_map(&s->vis);
+    s->vis_valid = false;
+    float locs[kMaxRecorders][3];
+    for (int32_t i = 0; i < nrec; ++i)
+      for (int k = 0; k < 3; ++k) locs[i][k] = recs[i].location[k];
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    // build peak: 24 bytes per entry for the sort plus the 8 kept; the
+    // automatic setting keeps at most EAR_VISMAP_AUTO_MAX_ENTRIES and
+    // lowers the resolution by a quarter until the lists fit
+    const uint64_t fit = (uint64_t)(free_b / 2) / 32;
+    const uint64_t limit = std::min<uint64_t>(
+        automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
+    char msg[256] = "";
+    bool too_large = false;
+    CU(cudaEventRecord(s->ev0, st));
+    for (;;) {
+      const cudaError_t e = build_vis_map(s->ds, locs, nrec, res, limit, st, &s->vis, &too_large,
+                                          msg, sizeof msg);
+      if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
+                    "visibility map build: %s", msg[0] ? msg : cudaGetErrorString(e));
+      if (!too_large || !automatic || res <= 64) break;
+      res = std::max(64, (res * 3 / 4) / 32 * 32);
+    }
+    CU(cudaEventRecord(s->ev1, st));
+    CU(cudaEventSynchronize(s->ev1));
+    float ms = 0.0f;
+    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    *build_ms = ms;
+    s->vis_refused = too_large;
+    s->vis_key = key;
+    s->vis_valid = true;
+  }
+  if (s->vis_refused) return EAR_OK;
+  a.vis_start = s->vis.start;
+  a.vis_entries = s->vis.entries;
+  a.vis_res = s->vis.res;
+  a.vis_cap = kVisWalkCap;
+  return EAR_OK;
+}
+
+void map_stats(const ear_scene* s, const TraceArgs& a, ear_render_stats* stats) {
+  stats->map_bytes = a.vis_res > 0 ? (uint64_t)s->vis.bytes : 0;
+  stats->map_res = a.vis_res;
+  stats->reserved1 = 0;
 }
 
 struct Prepared {
@@ -610,6 +693,9 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
   cudaStream_t st = (cudaStream_t)p->stream;
   rc = choose_visibility_order(s, recs, nrec, a, pr.ops, st);
   if (rc != EAR_OK) return rc;
+  double map_ms = 0.0;
+  rc = use_visibility_maps(s, recs, nrec, a, st, &map_ms);
+  if (rc != EAR_OK) return rc;
   CU(cudaEventRecord(s->ev0, st));
   // with no rays the launch still computes the direct-sound visibility
   CU(pr.ops->trace(a, a.num_items > 0 ? pr.grid : 1, pr.block, pr.smem, kModeForward, st));
@@ -677,7 +763,10 @@ extern "C" ear_status ear_render(ear_scene* s, const ear_source* src, const ear_
     stats->triangle_tests = cnt[kTriTests];
     stats->splat_bins = cnt[kSplatBins];
     stats->kernel_ms = ms;
-    }
+    stats->map_entries = cnt[kMapEntries];
+    stats->map_build_ms = map_ms;
+    map_stats(s, a, stats);
+  }
   return EAR_OK;
 }
 
@@ -692,6 +781,9 @@ extern "C" ear_status ear_trace_debug(ear_scene* s, const ear_source* src,
   ear_status rc = prepare(s, src, recs, nrec, p, 1u << band, &pr, kModeDebug);
   if (rc != EAR_OK) return rc;
   TraceArgs& a = pr.a;
+  double map_ms = 0.0;
+  rc = use_visibility_maps(s, recs, nrec, a, (cudaStream_t)p->stream, &map_ms);
+  if (rc != EAR_OK) return rc;
   const size_t n = (size_t)p->num_rays * (size_t)max_record;
   if (n > ((size_t)1 << 31)) return fail(EAR_ERR_INVALID_ARG, "debug record too large");
   int32_t* dh = nullptr;
@@ -789,6 +881,9 @@ extern "C" ear_status ear_render_adjoint(ear_scene* s, const ear_source* src,
   if (rc != EAR_OK) return rc;
   TraceArgs& a = pr.a;
   cudaStream_t st = (cudaStream_t)p->stream;
+  double map_ms = 0.0;
+  rc = use_visibility_maps(s, recs, nrec, a, st, &map_ms);
+  if (rc != EAR_OK) return rc;
   const int rows = pr.num_tracks * 3;
   // scaled upstream gradient in the (otherwise idle) histogram scratch
   float* g_in = nullptr;
@@ -848,7 +943,10 @@ extern "C" ear_status ear_render_adjoint(ear_scene* s, const ear_source* src,
     stats->triangle_tests = cnt[kTriTests];
     stats->splat_bins = cnt[kSplatBins];
     stats->kernel_ms = ms;
-    }
+    stats->map_entries = cnt[kMapEntries];
+    stats->map_build_ms = map_ms;
+    map_stats(s, a, stats);
+  }
   return EAR_OK;
 }
 
@@ -964,12 +1062,15 @@ ear_status ear_statistical_t60(const float* vertices, const int64_t* block_trian
 namespace {
 
 constexpr int kNoAllocScratchBytes = 16384;
-constexpr size_t kNaCounters = 0;      // 8 x u64 path counters
-constexpr size_t kNaError = 64;        // error flag
+constexpr size_t kNaCounters = 0;      // kNumCounters x u64 path counters
+constexpr size_t kNaError = 96;        // error flag
 constexpr size_t kNaRecs = 128;        // kMaxRecorders DevRecorder
 constexpr size_t kNaVis = kNaRecs + sizeof(DevRecorder) * kMaxRecorders;
 constexpr size_t kNaFirstLast = 2048;  // kMaxTracks x 3 int2
 static_assert(kNaVis + sizeof(int) * kMaxRecorders <= kNaFirstLast, "no-alloc scratch layout");
+static_assert(kNaCounters + sizeof(unsigned long long) * kNumCounters <= kNaError &&
+                  kNaError + sizeof(int) <= kNaRecs,
+              "no-alloc scratch layout");
 static_assert(kNaFirstLast + sizeof(int2) * 3 * kMaxTracks <= (size_t)kNoAllocScratchBytes,
               "no-alloc scratch layout");
 
@@ -1157,6 +1258,11 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     stats->triangle_tests = cnt[kTriTests];
     stats->splat_bins = cnt[kSplatBins];
     stats->kernel_ms = ms;
-    }
+    stats->map_entries = 0;  // the no-alloc path keeps the tree traversal
+    stats->map_build_ms = 0.0;
+    stats->map_bytes = 0;
+    stats->map_res = 0;
+    stats->reserved1 = 0;
+  }
   return EAR_OK;
 }

@@ -150,6 +150,12 @@ struct TraceArgs {
   int num_tracks;
   int2* first_last;  // [track][band]
   int* direct_vis;   // [recorder] direct-path visibility, or null
+  // listener visibility maps of the recorders (vis_res = 0: none); a cell
+  // holding more than vis_cap entries is left to the tree traversal
+  const uint32_t* vis_start;
+  const int2* vis_entries;
+  int vis_res;
+  int vis_cap;
   // adjoint mode: upstream gradient of the raw splat sums [track][band][stride]
   // and the gradient accumulators [material][band][2 = absorption, refraction]
   const float* adj_g;
@@ -181,7 +187,8 @@ enum Counter {
   kNodeVisits = 5,  // internal-node visits (64 B each)
   kTriTests = 6,    // Moller-Trumbore tests (48 B each)
   kSplatBins = 7,   // histogram bins written
-  kNumCounters = 8
+  kMapEntries = 8,  // visibility-map entries read (8 B each)
+  kNumCounters = 9
 };
 enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 
@@ -194,6 +201,32 @@ enum ErrorBits { kErrBudget = 1, kErrIndex = 2 };
 enum { kBuilderLbvh = 1, kBuilderPloc = 2 };
 cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder, int radius,
                        cudaStream_t stream, char* err, size_t errlen);
+
+// Listener visibility maps (vismap.cu): per recorder, a cube map of
+// res x res cells per face around its location; cell c lists, from
+// entries[start[c]] to entries[start[c+1]], (leaf position, distance bits)
+// of the triangles whose padded box meets the cell's cone of directions,
+// nearest first.  Cell index: ((recorder * 6 + face) * res + iv) * res + iu,
+// face = 2 * major axis + (major component < 0).
+struct VisMap {
+  uint32_t* start = nullptr;
+  int2* entries = nullptr;
+  int res = 0;
+  int num_recs = 0;
+  uint64_t num_entries = 0;
+  size_t bytes = 0;
+};
+// Cell of the direction ratio u in [-1, 1]; monotonic in u.
+__host__ __device__ __forceinline__ int vis_cell(float u, int res) {
+  const int i = (int)((u + 1.0f) * (0.5f * (float)res));
+  return i < 0 ? 0 : (i >= res ? res - 1 : i);
+}
+// Builds the maps of nrec recorder locations.  `too_large` is set (and no
+// map built) when the lists would hold more than max_entries entries.
+cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec, int res,
+                          uint64_t max_entries, cudaStream_t st, VisMap* out, bool* too_large,
+                          char* err, size_t errlen);
+void free_vis_map(VisMap* m);
 
 // Trace launches, one set per instantiation (trace_exact.cu, trace_fast.cu).
 // kModeBatch traces many jobs (scene, source, recorders) from one work

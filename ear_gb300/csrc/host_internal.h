@@ -120,4 +120,10 @@ struct ear_scene {
   unsigned* probe = nullptr;
   uint64_t probe_key = 0;
   bool probe_valid = false;
+  // listener visibility maps of one recorder set (ear_bvh_opts.visibility_map)
+  int vis_opt = 0;
+  ear::VisMap vis;
+  uint64_t vis_key = 0;
+  bool vis_valid = false;   // `vis` (or vis_refused) belongs to vis_key
+  bool vis_refused = false;  // the set's lists were above the entry limit
 };

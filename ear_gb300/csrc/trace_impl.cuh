@@ -147,7 +147,7 @@ struct Hit {
 };
 
 struct LaneCounters {
-  uint32_t segments, shadow, contrib, overflow, nodes, tris, bins;
+  uint32_t segments, shadow, contrib, overflow, nodes, tris, bins, map;
 };
 
 // Indices read from device data (child and parent links, leaf ranges, hit
@@ -598,6 +598,61 @@ struct Vertex {
   bool conn;     // connect the recorders at this vertex
 };
 
+// Visibility test of the segment from `o` to recorder `ri` (sdir = its
+// location - o, len = |sdir|) through the recorder's visibility map: the
+// entries of the cell of direction o - location nearer than the vertex, each
+// by the tree's own leaf test.  Returns 1 blocked, 0 clear, -1 when the map
+// leaves the test to the tree (degenerate direction, or a cell longer than
+// vis_cap).  The result equals the tree traversal's: the entries are every
+// triangle whose padded box meets the segment.
+__device__ __forceinline__ int vis_map_test(const TraceArgs& a, const SceneRef& S, int ri, V3 o,
+                                            V3 sdir, float len, Hit& h, LaneCounters& c,
+                                            int& err) {
+  const float qx = -sdir.x, qy = -sdir.y, qz = -sdir.z;
+  const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
+  int f;
+  float m, u, v;
+  if (ax >= ay && ax >= az) {
+    f = qx > 0.0f ? 0 : 1;
+    m = ax;
+    u = qy;
+    v = qz;
+  } else if (ay >= az) {
+    f = qy > 0.0f ? 2 : 3;
+    m = ay;
+    u = qx;
+    v = qz;
+  } else {
+    f = qz > 0.0f ? 4 : 5;
+    m = az;
+    u = qx;
+    v = qy;
+  }
+  if (!(m > 0.0f)) return -1;
+  const int res = a.vis_res;
+  const uint32_t cell = ((uint32_t)(ri * 6 + f) * (uint32_t)res + (uint32_t)vis_cell(v / m, res)) *
+                            (uint32_t)res +
+                        (uint32_t)vis_cell(u / m, res);
+  const uint32_t b = __ldg(a.vis_start + cell), e = __ldg(a.vis_start + cell + 1);
+  if (e - b > (uint32_t)a.vis_cap) return -1;
+  // entries are ordered by their boxes' distance from the recorder; a hit
+  // point of the segment lies nearer than len (t > 1e-5)
+  const float cut = len * 1.000244140625f;
+  uint32_t i = b;
+  bool blocked = false;
+  for (; i < e; ++i) {
+    const int2 en = __ldg(a.vis_entries + i);
+    if (__int_as_float(en.y) > cut) break;
+    if (leaf_test<true>(S, ~en.x, o, sdir, h, c, err)) {
+      blocked = true;
+      ++i;
+      break;
+    }
+  }
+  c.map += i - b;
+  return blocked ? 1 : 0;
+}
+
 // Visibility + contribution of recorder `ri` at the current vertex
 // (src/Scene.cpp:188-268).  Returns kNotTested, kBlockedSeg or kVisible.
 enum { kNotTested = 0, kBlockedSeg = 1, kVisible = 2 };
@@ -621,7 +676,10 @@ __device__ __forceinline__ int connect_one(const TraceArgs& a, const SceneRef* s
   Hit hh;
   const SceneRef S = scene_of<MODE>(a, s_scenes, st);
   const float slack = kSlackRel + S.box_pad / len;
-  if (traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err)) return kBlockedSeg;
+  int vm = -1;
+  if (MODE != kModeBatch && a.vis_res > 0) vm = vis_map_test(a, S, ri, st.o, sdir, len, hh, c, err);
+  if (vm < 0) vm = traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err) ? 1 : 0;
+  if (vm) return kBlockedSeg;
   if (!(dt > 0)) return kVisible;
   // sample_intensity_before_bounce (src/Scene.cpp:173): the path's
   // intensity, unchanged between the vertex and its connections
@@ -849,7 +907,7 @@ __device__ void direct_visibility(const TraceArgs& a, const SceneRef* s_scenes, 
     const V3 seg = sub(mk(src[0], src[1], src[2]), loc);
     const float seglen = length(seg);
     const float slack = kSlackRel + (seglen > 0.0f ? S.box_pad / seglen : 0.0f);
-    LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
+    LaneCounters c = {0, 0, 0, 0, 0, 0, 0, 0};
     Hit hh;
     const bool blocked = traverse<true>(S, loc, seg, 1.0f, slack, hh, c, err);
     a.direct_vis[r] = blocked ? 0 : 1;
@@ -901,7 +959,7 @@ __global__ void __launch_bounds__(kTraceMaxBlock, 4) trace_kernel(const TraceArg
   __syncthreads();
   if (MODE == kModeBatch) direct_visibility<MODE>(a, s_scenes, err);
   const int lane = threadIdx.x & 31;
-  LaneCounters c = {0, 0, 0, 0, 0, 0, 0};
+  LaneCounters c = {0, 0, 0, 0, 0, 0, 0, 0};
   bool alive = false, exhausted = false;
   PathState st;
   st.k = 0;
@@ -1010,11 +1068,13 @@ __global__ void __launch_bounds__(kTraceMaxBlock, 4) trace_kernel(const TraceArg
     const unsigned long long nv = __reduce_add_sync(kFull, c.nodes);
     const unsigned long long tt = __reduce_add_sync(kFull, c.tris);
     const unsigned long long bn = __reduce_add_sync(kFull, c.bins);
+    const unsigned long long me = __reduce_add_sync(kFull, c.map);
     const int werr = (int)__reduce_or_sync(kFull, (unsigned)err);
     if (lane == 0) {
       atomicAdd(a.counters + kNodeVisits, nv);
       atomicAdd(a.counters + kTriTests, tt);
       atomicAdd(a.counters + kSplatBins, bn);
+      if (me) atomicAdd(a.counters + kMapEntries, me);
       atomicAdd(a.counters + kSegments, (unsigned long long)seg);
       atomicAdd(a.counters + kShadow, (unsigned long long)sh);
       atomicAdd(a.counters + kContrib, (unsigned long long)co);

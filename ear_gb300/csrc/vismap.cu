@@ -1,0 +1,381 @@
+// vismap.cu -- listener visibility maps: an exact accelerator for the
+// visibility (any-hit) tests between path vertices and recorders.
+//
+// Every path vertex tests the segment to each recorder with
+// Mesh::LineIntersection (src/Scene.cpp:188-190, src/Mesh.cpp:58-71).  All
+// of a recorder's segments end at the same point, so they can be binned by
+// direction around it: a cube map of res x res cells per face, and per cell
+// the list of triangles whose padded bounding box meets the cell's cone of
+// directions, sorted by the box's distance from the recorder.  A test then
+// reads the cell of its direction and runs the ordinary triangle test on
+// the entries nearer than the vertex, instead of descending the tree from
+// its root.
+//
+// The lists are conservative, so the result is the tree traversal's bit
+// for bit: the traversal already relies on every point where the triangle
+// test can report a hit lying inside the triangle's box padded by box_pad;
+// here the boxes are padded by 2 box_pad, which also covers the rounding
+// of the segment's direction.  A box's cells are bounded in closed form:
+// over a box's points with major coordinate a in (max(a0, 0), a1] and
+// minor coordinate y in [y0, y1] the ratio y / a ranges from y0 / a1 (y0 >=
+// 0) or y0 / max(a0, 0) (y0 < 0) to y1 / a1 (y1 <= 0) or y1 / max(a0, 0)
+// (y1 > 0), unbounded where max(a0, 0) = 0.  Both the bounds and the
+// queries go through vis_cell(), which is monotonic, with a relative margin
+// of 2e-6 on the bounds against the rounding of the divisions.  Where a
+// triangle lies wholly in front of a face, its cells are further limited
+// to those meeting its projection widened by the padding's angular size
+// (tri_proj, cell_meets).
+//
+// Compiled with --fmad=false: the count and fill passes must compute the
+// same cells.
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <stdio.h>
+
+#include <algorithm>
+
+#include "ear_internal.h"
+
+namespace ear {
+namespace {
+
+struct VisBuildArgs {
+  float loc[kMaxRecorders][3];
+  int nrec;
+  int res;
+  float pad;
+  const float4* tris;   // leaf order; .w of the first float4 = file-order index
+  const float* verts;   // [n][9], file order
+  int num_tris;
+};
+
+struct FaceRect {
+  int u0, u1, v0, v1;
+};
+
+__device__ __forceinline__ void ratio_range(float y0, float y1, float xa, float a1, float& lo,
+                                            float& hi) {
+  lo = y0 >= 0.0f ? y0 / a1 : (xa > 0.0f ? y0 / xa : -INFINITY);
+  hi = y1 <= 0.0f ? y1 / a1 : (xa > 0.0f ? y1 / xa : INFINITY);
+  lo -= 2e-6f + 2e-6f * fabsf(lo);
+  hi += 2e-6f + 2e-6f * fabsf(hi);
+  lo = fmaxf(lo, -1.0f);
+  hi = fminf(hi, 1.0f);
+}
+
+// Cells of face f met by the box [lo, hi] (coordinates relative to the
+// recorder).  Faces: 2 * axis + (negative side).
+__device__ __forceinline__ bool face_rect(const float* lo, const float* hi, int f, int res,
+                                          FaceRect& r) {
+  const int m = f >> 1;
+  const bool neg = f & 1;
+  const float a0 = neg ? -hi[m] : lo[m];
+  const float a1 = neg ? -lo[m] : hi[m];
+  if (!(a1 > 0.0f)) return false;
+  const float xa = fmaxf(a0, 0.0f);
+  const int p = m == 0 ? 1 : 0;
+  const int q = m == 2 ? 1 : 2;
+  float ulo, uhi, vlo, vhi;
+  ratio_range(lo[p], hi[p], xa, a1, ulo, uhi);
+  ratio_range(lo[q], hi[q], xa, a1, vlo, vhi);
+  if (!(ulo <= uhi) || !(vlo <= vhi)) return false;
+  r.u0 = vis_cell(ulo, res);
+  r.u1 = vis_cell(uhi, res);
+  r.v0 = vis_cell(vlo, res);
+  r.v1 = vis_cell(vhi, res);
+  return true;
+}
+
+// Padded box of the triangle at leaf position `pos`, relative to recorder
+// `ri`, its distance from the recorder (rounded down) and the relative
+// vertices t[3][3].
+__device__ __forceinline__ float rel_box(const VisBuildArgs& a, int ri, int pos, float* lo,
+                                         float* hi, float (*t)[3]) {
+  const int orig = __float_as_int(__ldg(&a.tris[4 * (size_t)pos].w));
+  const float* v = a.verts + 9 * (size_t)orig;
+  float d2 = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    const float x0 = __ldg(v + k), x1 = __ldg(v + 3 + k), x2 = __ldg(v + 6 + k);
+    lo[k] = (fminf(fminf(x0, x1), x2) - a.pad) - a.loc[ri][k];
+    hi[k] = (fmaxf(fmaxf(x0, x1), x2) + a.pad) - a.loc[ri][k];
+    t[0][k] = x0 - a.loc[ri][k];
+    t[1][k] = x1 - a.loc[ri][k];
+    t[2][k] = x2 - a.loc[ri][k];
+    const float g = fmaxf(fmaxf(lo[k], -hi[k]), 0.0f);
+    d2 += g * g;
+  }
+  return sqrtf(d2) * 0.99999f;
+}
+
+// The triangle seen from the recorder on face f: where all three vertices
+// lie beyond the padding in front of the face, the directions of the
+// padded triangle T + [-P, P]^3 fall inside the projected triangle
+// (u_i, v_i) = (y_i, z_i) / a_i widened by du = P (1 + max |u_i|) /
+// (min a_i - P) (and dv alike): u(t + d) - u(t) = (d_y - u(t) d_a) /
+// (t_a + d_a).  P carries a tenth more for the rounding of the relative
+// vertices, the widths 1e-5 more for the divisions.
+struct TriProj {
+  float u[3], v[3];
+  float du, dv;
+  float umin, umax, vmin, vmax;
+  float eps;  // bound on the rounding of u_i, v_i (relative 1e-6 of the largest)
+};
+
+__device__ __forceinline__ bool tri_proj(const float (*t)[3], int f, float pad, TriProj& tp) {
+  const int m = f >> 1;
+  const bool neg = f & 1;
+  const int p = m == 0 ? 1 : 0;
+  const int q = m == 2 ? 1 : 2;
+  const float P = pad * 1.1f;
+  float amin = INFINITY, mu = 0.0f, mv = 0.0f;
+  float ai[3];
+  for (int i = 0; i < 3; ++i) {
+    ai[i] = neg ? -t[i][m] : t[i][m];
+    amin = fminf(amin, ai[i]);
+  }
+  if (!(amin > 2.0f * P)) return false;
+  tp.umin = tp.vmin = INFINITY;
+  tp.umax = tp.vmax = -INFINITY;
+  for (int i = 0; i < 3; ++i) {
+    tp.u[i] = t[i][p] / ai[i];
+    tp.v[i] = t[i][q] / ai[i];
+    mu = fmaxf(mu, fabsf(tp.u[i]));
+    mv = fmaxf(mv, fabsf(tp.v[i]));
+    tp.umin = fminf(tp.umin, tp.u[i]);
+    tp.umax = fmaxf(tp.umax, tp.u[i]);
+    tp.vmin = fminf(tp.vmin, tp.v[i]);
+    tp.vmax = fmaxf(tp.vmax, tp.v[i]);
+  }
+  const float den = amin - P;
+  tp.du = P * (1.0f + mu) / den * 1.0001f + 1e-5f;
+  tp.dv = P * (1.0f + mv) / den * 1.0001f + 1e-5f;
+  tp.eps = 1e-6f * (1.0f + fmaxf(mu, mv));
+  return true;
+}
+
+// Does cell (iu, iv) meet the widened projected triangle?  Separating axes:
+// the cell's own (the triangle's bounding box) and the three edge normals.
+// An edge function n . (c - P_i) moves by at most 2 eps (|c - P_i| + |P_j -
+// P_i|) when the vertices move by eps, so a corner separates only beyond
+// that (plus the products' rounding); an edge whose orientation the same
+// bound leaves open (a sliver seen edge-on) never separates.
+__device__ __forceinline__ bool cell_meets(const TriProj& tp, int iu, int iv, int res) {
+  const float w = 2.0f / (float)res;
+  const float x0 = (-1.0f + (float)iu * w) - tp.du, x1 = (-1.0f + (float)(iu + 1) * w) + tp.du;
+  const float y0 = (-1.0f + (float)iv * w) - tp.dv, y1 = (-1.0f + (float)(iv + 1) * w) + tp.dv;
+  if (x1 < tp.umin || x0 > tp.umax || y1 < tp.vmin || y0 > tp.vmax) return false;
+  for (int e = 0; e < 3; ++e) {
+    const int i = e, j = e == 2 ? 0 : e + 1, k = e == 0 ? 2 : e - 1;
+    float nx = -(tp.v[j] - tp.v[i]), ny = tp.u[j] - tp.u[i];
+    const float len = fabsf(nx) + fabsf(ny);
+    const float dk = fabsf(tp.u[k] - tp.u[i]) + fabsf(tp.v[k] - tp.v[i]);
+    const float side = nx * (tp.u[k] - tp.u[i]) + ny * (tp.v[k] - tp.v[i]);
+    if (!(fabsf(side) > 2.0f * tp.eps * (dk + len) + 1e-6f * len * dk)) continue;
+    if (side < 0.0f) {
+      nx = -nx;
+      ny = -ny;
+    }
+    const float cu = nx > 0.0f ? x1 : x0, cv = ny > 0.0f ? y1 : y0;
+    const float reach = nx * (cu - tp.u[i]) + ny * (cv - tp.v[i]);
+    const float dc = fabsf(cu - tp.u[i]) + fabsf(cv - tp.v[i]);
+    if (reach < -(2.0f * tp.eps * (dc + len) + 1e-6f * len * dc)) return false;
+  }
+  return true;
+}
+
+__global__ void k_vis_count(const VisBuildArgs a, uint64_t* __restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)a.nrec * a.num_tris) return;
+  const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
+  float lo[3], hi[3], t[3][3];
+  rel_box(a, ri, pos, lo, hi, t);
+  uint64_t n = 0;
+  for (int f = 0; f < 6; ++f) {
+    FaceRect r;
+    if (!face_rect(lo, hi, f, a.res, r)) continue;
+    TriProj tp;
+    if (!tri_proj(t, f, a.pad, tp)) {
+      n += (uint64_t)(r.u1 - r.u0 + 1) * (uint64_t)(r.v1 - r.v0 + 1);
+      continue;
+    }
+    for (int v = r.v0; v <= r.v1; ++v)
+      for (int u = r.u0; u <= r.u1; ++u) n += cell_meets(tp, u, v, a.res) ? 1u : 0u;
+  }
+  count[i] = n;
+}
+
+__global__ void k_vis_fill(const VisBuildArgs a, const uint64_t* __restrict__ count,
+                           const uint64_t* __restrict__ offset, uint64_t* __restrict__ keys,
+                           int32_t* __restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)a.nrec * a.num_tris) return;
+  const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
+  float lo[3], hi[3], t[3][3];
+  const float dist = rel_box(a, ri, pos, lo, hi, t);
+  const uint64_t cells_per_rec = 6ull * a.res * a.res;
+  const uint64_t n = count[i];
+  uint64_t o = offset[i], w = 0;
+  const uint64_t dbits = __float_as_uint(dist);
+  for (int f = 0; f < 6; ++f) {
+    FaceRect r;
+    if (!face_rect(lo, hi, f, a.res, r)) continue;
+    TriProj tp;
+    const bool tri = tri_proj(t, f, a.pad, tp);
+    for (int v = r.v0; v <= r.v1; ++v)
+      for (int u = r.u0; u <= r.u1 && w < n; ++u) {
+        if (tri && !cell_meets(tp, u, v, a.res)) continue;
+        const uint64_t cell = ri * cells_per_rec + ((uint64_t)f * a.res + v) * a.res + u;
+        keys[o + w] = (cell << 32) | dbits;
+        vals[o + w] = pos;
+        ++w;
+      }
+  }
+  // never reached with --fmad=false (both passes compute the same cells);
+  // keeps every slot defined: past the last cell, dropped by the bounds
+  for (; w < n; ++w) {
+    keys[o + w] = ((uint64_t)a.nrec * cells_per_rec) << 32;
+    vals[o + w] = 0;
+  }
+}
+
+// start[c] = first entry of cell c (c = 0 .. cells): binary search.
+__global__ void k_vis_start(const uint64_t* __restrict__ keys, int64_t n, uint64_t cells,
+                            uint32_t* __restrict__ start) {
+  const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > cells) return;
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((keys[mid] >> 32) < c)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  start[c] = (uint32_t)lo;
+}
+
+__global__ void k_vis_pack(const uint64_t* __restrict__ keys, const int32_t* __restrict__ vals,
+                           int64_t n, int2* __restrict__ entries) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  entries[i] = make_int2(vals[i], (int)(uint32_t)keys[i]);
+}
+
+int bits_for(uint64_t v) {
+  int b = 0;
+  while (b < 64 && (v >> b)) ++b;
+  return b;
+}
+
+}  // namespace
+
+void free_vis_map(VisMap* m) {
+  cudaFree(m->start);
+  cudaFree(m->entries);
+  *m = VisMap{};
+}
+
+#define VCK(x)                                                                    \
+  do {                                                                            \
+    cudaError_t e_ = (x);                                                         \
+    if (e_ != cudaSuccess) {                                                      \
+      snprintf(err, errlen, "%s: %s", #x, cudaGetErrorString(e_));                \
+      rc = e_;                                                                    \
+      goto done;                                                                  \
+    }                                                                             \
+  } while (0)
+
+cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec, int res,
+                          uint64_t max_entries, cudaStream_t st, VisMap* out, bool* too_large,
+                          char* err, size_t errlen) {
+  *too_large = false;
+  *out = VisMap{};
+  cudaError_t rc = cudaSuccess;
+  VisBuildArgs a = {};
+  uint64_t *count = nullptr, *offset = nullptr, *keys = nullptr, *keys2 = nullptr;
+  int32_t *vals = nullptr, *vals2 = nullptr;
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0, need = 0;
+  uint64_t total = 0, last_count = 0;
+  const int64_t items = (int64_t)nrec * s.num_tris;
+  const uint64_t cells = 6ull * res * res * (uint64_t)nrec;
+  constexpr int B = 256;
+  if (nrec <= 0 || nrec > kMaxRecorders || res <= 0 || res > 4096 || s.num_tris <= 0 ||
+      s.num_tris > kLeafStartMask || cells >= (1ull << 31)) {
+    snprintf(err, errlen, "visibility map: bad sizes");
+    return cudaErrorInvalidValue;
+  }
+  for (int r = 0; r < nrec; ++r)
+    for (int k = 0; k < 3; ++k) a.loc[r][k] = locs[r][k];
+  a.nrec = nrec;
+  a.res = res;
+  a.pad = 2.0f * s.box_pad;
+  a.tris = s.tris;
+  a.verts = s.vertices;
+  a.num_tris = (int)s.num_tris;
+  {
+    VCK(cudaMalloc(&count, sizeof(uint64_t) * items));
+    VCK(cudaMalloc(&offset, sizeof(uint64_t) * items));
+    const unsigned g = (unsigned)((items + B - 1) / B);
+    k_vis_count<<<g, B, 0, st>>>(a, count);
+    VCK(cudaGetLastError());
+    VCK(cub::DeviceScan::ExclusiveSum(nullptr, need, count, offset, items, st));
+    VCK(cudaMalloc(&tmp, need));
+    tmp_bytes = need;
+    VCK(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, offset, items, st));
+    VCK(cudaMemcpyAsync(&total, offset + items - 1, sizeof total, cudaMemcpyDeviceToHost, st));
+    VCK(cudaMemcpyAsync(&last_count, count + items - 1, sizeof last_count, cudaMemcpyDeviceToHost, st));
+    VCK(cudaStreamSynchronize(st));
+    total += last_count;
+    if (total > max_entries || total >= (1ull << 31)) {
+      *too_large = true;
+      snprintf(err, errlen, "visibility map: %llu entries above the limit of %llu",
+               (unsigned long long)total, (unsigned long long)max_entries);
+      goto done;
+    }
+    cudaFree(tmp);
+    tmp = nullptr;
+    const int64_t n = (int64_t)total;
+    VCK(cudaMalloc(&keys, sizeof(uint64_t) * std::max<int64_t>(n, 1)));
+    VCK(cudaMalloc(&keys2, sizeof(uint64_t) * std::max<int64_t>(n, 1)));
+    VCK(cudaMalloc(&vals, sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    VCK(cudaMalloc(&vals2, sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    k_vis_fill<<<g, B, 0, st>>>(a, count, offset, keys, vals);
+    VCK(cudaGetLastError());
+    cub::DoubleBuffer<uint64_t> dk(keys, keys2);
+    cub::DoubleBuffer<int32_t> dv(vals, vals2);
+    const int end_bit = 32 + bits_for(cells);
+    need = 0;
+    VCK(cub::DeviceRadixSort::SortPairs(nullptr, need, dk, dv, (int)n, 0, end_bit, st));
+    VCK(cudaMalloc(&tmp, std::max<size_t>(need, 1)));
+    tmp_bytes = need;
+    VCK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, dk, dv, (int)n, 0, end_bit, st));
+    VCK(cudaMalloc(&out->start, sizeof(uint32_t) * (cells + 1)));
+    VCK(cudaMalloc(&out->entries, sizeof(int2) * std::max<int64_t>(n, 1)));
+    k_vis_start<<<(unsigned)((cells + 1 + B - 1) / B), B, 0, st>>>(dk.Current(), n, cells, out->start);
+    VCK(cudaGetLastError());
+    if (n > 0) {
+      k_vis_pack<<<(unsigned)((n + B - 1) / B), B, 0, st>>>(dk.Current(), dv.Current(), n, out->entries);
+      VCK(cudaGetLastError());
+    }
+    VCK(cudaStreamSynchronize(st));
+    out->res = res;
+    out->num_recs = nrec;
+    out->num_entries = (uint64_t)n;
+    out->bytes = sizeof(uint32_t) * (cells + 1) + sizeof(int2) * (size_t)n;
+  }
+done:
+  cudaFree(count);
+  cudaFree(offset);
+  cudaFree(keys);
+  cudaFree(keys2);
+  cudaFree(vals);
+  cudaFree(vals2);
+  cudaFree(tmp);
+  if (rc != cudaSuccess || *too_large) free_vis_map(out);
+  return rc;
+}
+
+}  // namespace ear

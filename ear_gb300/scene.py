@@ -150,7 +150,8 @@ class Tracer:
 
     def __init__(self, vertices, material_ids, materials: Sequence[Material], device: int = 0,
                  box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
-                 ploc_radius: int = 0, width: int = 0, visibility_order: int = 0):
+                 ploc_radius: int = 0, width: int = 0, visibility_order: int = 0,
+                 visibility_map: int = 0):
         L = N.lib()
         self._v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
         self._m = np.ascontiguousarray(material_ids, dtype=np.int32).reshape(-1)
@@ -171,13 +172,18 @@ class Tracer:
         N.check(L.ear_scene_create(C.byref(desc), C.byref(h)))
         self._h = h
         self.build_bvh(box_pad=box_pad, builder=builder, max_leaf=max_leaf,
-                       ploc_radius=ploc_radius, width=width, visibility_order=visibility_order)
+                       ploc_radius=ploc_radius, width=width, visibility_order=visibility_order,
+                       visibility_map=visibility_map)
 
     def build_bvh(self, box_pad: float = -1.0, builder: str = "default", max_leaf: int = 0,
-                  ploc_radius: int = 0, width: int = 0, visibility_order: int = 0) -> None:
+                  ploc_radius: int = 0, width: int = 0, visibility_order: int = 0,
+                  visibility_map: int = 0) -> None:
         """(Re)build the BVH: builder "default", "lbvh" or "ploc"; traversal
         width 2, 4 or 0 (4-wide from 4096 triangles); visibility_order 1
-        nearest first, 2 farthest first, 0 automatic."""
+        nearest first, 2 farthest first, 0 automatic; visibility_map -1 off,
+        8..2048 on with that many cells per cube-face edge, 0 automatic
+        (listener visibility maps: visibility tests by direction lists
+        around each recorder instead of tree traversals)."""
         opts = N.EarBvhOpts()
         opts.box_pad = float(box_pad)
         opts.max_leaf_size = int(max_leaf)
@@ -186,6 +192,7 @@ class Tracer:
         opts.ploc_radius = int(ploc_radius)
         opts.width = int(width)
         opts.visibility_order = int(visibility_order)
+        opts.visibility_map = int(visibility_map)
         N.check(N.lib().ear_scene_build_bvh(self._h, C.byref(opts)))
         self._width = int(width) if width else (4 if self.num_triangles >= 4096 else 2)
         self._builder = builder

@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define EAR_ABI_VERSION 1
+#define EAR_ABI_VERSION 2
 #define EAR_NUM_BANDS 3
 #define EAR_SAMPLE_RATE 44100
 /* Loop bound of Scene::Render: 1000 iterations = emission + 999 reflections
@@ -120,8 +120,22 @@ typedef struct ear_bvh_opts {
      finds more than 15% of 8192 segments between triangle pairs blocked.
      Never changes a result. */
   int32_t visibility_order;
-  int32_t reserved[2];
+  /* Listener visibility maps: per recorder location, a cube map of
+     directions around it whose cells list the triangles (padded boxes) in
+     their cone, nearest first.  A visibility test then runs the triangle
+     test on its cell's entries nearer than the path vertex instead of
+     traversing the tree; cells longer than a limit, and batched renders,
+     keep the traversal.  Built on a render's first use of a recorder set
+     and kept until the set, the tree or this setting changes.  > 0: on,
+     with this many cells per face edge (8..2048); -1: off; 0 = automatic:
+     on, with 4 sqrt(triangles) cells per edge (a multiple of 64,
+     64..2048), lowered while the lists would hold more than
+     EAR_VISMAP_AUTO_MAX_ENTRIES entries.  Never changes a result. */
+  int32_t visibility_map;
+  int32_t reserved;
 } ear_bvh_opts;
+
+#define EAR_VISMAP_AUTO_MAX_ENTRIES (1ull << 30) /* 8 GiB of lists */
 
 #define EAR_BVH_DEFAULT 0
 #define EAR_BVH_LBVH 1
@@ -186,6 +200,13 @@ typedef struct ear_render_stats {
   uint64_t triangle_tests; /* ray/triangle tests (48 bytes of geometry each) */
   uint64_t splat_bins;     /* histogram bins written by splats */
   double kernel_ms;        /* device time of the trace kernel(s) */
+  uint64_t map_entries;    /* listener visibility-map entries read (8 bytes
+                              each; see ear_bvh_opts.visibility_map) */
+  double map_build_ms;     /* time this call spent building visibility maps
+                              (0 when they were reused or are off) */
+  uint64_t map_bytes;      /* device bytes of the maps in use (0: none) */
+  int32_t map_res;         /* their cells per face edge (0: none) */
+  int32_t reserved1;
 } ear_render_stats;
 
 typedef struct ear_histograms {

@@ -68,7 +68,7 @@ def test_ctypes_layout_matches_c():
 
 def test_version_and_errors_without_gpu():
     L = N.lib()
-    assert L.ear_abi_version() == 1
+    assert L.ear_abi_version() == 2
     assert b"sm_103a" in L.ear_version()
     h = C.c_void_p()
     assert L.ear_scene_create(None, C.byref(h)) == N.EAR_ERR_INVALID_ARG
