@@ -45,8 +45,6 @@ thread_local char g_err[512] = "";
 // (measured +4..6% segments/s over the LBVH on the 20,000- and
 // 2,000,000-triangle scenes).
 constexpr int kDefaultBuilder = EAR_BVH_PLOC;
-// Visibility-map cells with more entries than this are left to the tree.
-constexpr int kVisWalkCap = 96;
 
 ear_status fail(ear_status st, const char* fmt, ...) {
   va_list ap;
@@ -98,6 +96,7 @@ int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job
     d.channels = r.channels;
     d.track0 = track_base + tracks;
     d.job = job;
+    d.vis_index = i;
     tracks += r.channels;
     out->push_back(d);
   }
@@ -118,6 +117,9 @@ void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel
   stats->kernel_ms = kernel_ms;
   stats->map_entries = cnt[kMapEntries];
   stats->map_build_ms = 0.0;
+  stats->map_bytes = 0;
+  stats->map_res = 0;
+  stats->reserved1 = 0;
 }
 
 namespace fin {
@@ -308,6 +310,7 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   s->vis_opt = vmap;
   free_vis_map(&s->vis);
   s->vis_valid = false;
+  ++s->bvh_gen;
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
@@ -479,11 +482,9 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
   if (nrec <= 0 || s->vis_opt < 0 || s->ds.num_tris <= 0) return EAR_OK;
   const bool automatic = s->vis_opt == 0;
   int res = s->vis_opt;
-  if (automatic) {
-    const double r = 4.0 * std::sqrt((double)s->ds.num_tris);
-    res = (int)std::min(2048.0, std::max(64.0, std::floor(r / 64.0) * 64.0));
-  }
-  uint64_t key = 1469598103934665603ull ^ (uint64_t)res;
+  if (automatic) res = vis_auto_res(s->ds.num_tris);
+  uint64_t key = (1469598103934665603ull ^ (uint64_t)res) * 1099511628211ull;
+  key = (key ^ s->bvh_gen) * 1099511628211ull;
   for (int32_t i = 0; i < nrec; ++i)
     for (int k = 0; k < 3; ++k) {
       uint32_t bits;
@@ -492,6 +493,9 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
     }
   key = (key ^ (uint64_t)nrec) * 1099511628211ull;
   if (!s->vis_valid || key != s->vis_key) {
+    // automatic: a render of fewer paths than the scene has triangles
+    // does not repay the build (a new recorder set per short render)
+    if (automatic && a.num_items < (uint64_t)s->ds.num_tris) return EAR_OK;
     free_vis_map(&s->vis);
     s->vis_valid = false;
     float locs[kMaxRecorders][3];

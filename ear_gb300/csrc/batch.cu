@@ -67,6 +67,12 @@ struct ear_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // listener visibility maps, one per scene over the distinct recorder
+  // locations of its jobs, and the tree generation / setting they follow
+  std::vector<VisMap> maps;
+  std::vector<uint64_t> map_gen;
+  std::vector<int> map_opt;
+  double map_build_ms = 0.0;  // spent since the last run
   // results of the last run
   std::vector<int2> fl;
   bool ran = false;
@@ -83,8 +89,9 @@ void free_graph(ear_batch* b) {
   b->graph = nullptr;
 }
 
-SceneRef scene_ref(const ear_scene* s, int mat_base) {
+SceneRef scene_ref(const ear_scene* s, int mat_base, const VisMap& m) {
   SceneRef r;
+  std::memset(&r, 0, sizeof r);  // the table is compared bytewise
   r.nodes2 = s->ds.nodes;
   r.nodes4 = s->ds.nodes4;
   r.wide = s->ds.wide;
@@ -97,16 +104,108 @@ SceneRef scene_ref(const ear_scene* s, int mat_base) {
   r.mat_base = mat_base;
   r.num_mats = s->num_mats;
   r.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
+  r.vis_start = m.start;
+  r.vis_entries = m.entries;
+  r.vis_res = m.start ? m.res : 0;
+  r.vis_cap = kVisWalkCap;
   return r;
 }
 
-// Re-reads the scenes' device pointers (a BVH rebuild replaces them); a
-// change re-uploads the scene table and drops the captured graph.
+// Most cells of one scene's automatic maps in a batch (256 MiB of list
+// starts): the resolution drops as the scene's recorder count grows.
+constexpr uint64_t kBatchMapCells = 1ull << 26;
+
+// (Re)builds the visibility maps of the scenes whose tree or setting
+// changed: one map per scene over the distinct locations of its jobs'
+// recorders (more than kMaxRecorders keep the tree).  Automatic setting:
+// when the scene's jobs trace at least as many paths as it has
+// triangles, at the single-render resolution capped by kBatchMapCells and
+// lowered while the lists exceed EAR_VISMAP_AUTO_MAX_ENTRIES.  Each
+// recorder's vis_index names its list set (-1: no map).
+ear_status build_batch_maps(ear_batch* b) {
+  const size_t ns = b->scenes.size();
+  b->maps.resize(ns);
+  b->map_gen.resize(ns, ~0ull);
+  b->map_opt.resize(ns, 0);
+  int nb = 0;
+  for (int k = 0; k < 3; ++k) nb += (b->params.bands_mask >> k) & 1;
+  bool recs_changed = false;
+  cudaStream_t st = (cudaStream_t)b->params.stream;
+  for (size_t i = 0; i < ns; ++i) {
+    ear_scene* s = b->scenes[i];
+    if (b->map_gen[i] == s->bvh_gen && b->map_opt[i] == s->vis_opt) continue;
+    free_vis_map(&b->maps[i]);
+    b->map_gen[i] = s->bvh_gen;
+    b->map_opt[i] = s->vis_opt;
+    recs_changed = true;
+    std::vector<float> locs;  // distinct locations, 3 floats each
+    std::vector<int> index(b->recs.size(), -1);
+    uint64_t work = 0;
+    for (const BatchJob& j : b->jobs) {
+      if ((size_t)j.scene != i) continue;
+      work += j.num_rays * (uint64_t)nb;
+      for (int r = j.rec_base; r < j.rec_base + j.num_recs; ++r) {
+        const float* l = b->recs[(size_t)r].loc;
+        size_t k = 0;
+        while (k < locs.size() / 3 && std::memcmp(&locs[3 * k], l, 3 * sizeof(float)) != 0) ++k;
+        if (k == locs.size() / 3) locs.insert(locs.end(), l, l + 3);
+        index[(size_t)r] = (int)k;
+      }
+    }
+    const int nloc = (int)(locs.size() / 3);
+    const bool automatic = s->vis_opt == 0;
+    int res = automatic ? vis_auto_res(s->ds.num_tris) : s->vis_opt;
+    bool use = s->vis_opt >= 0 && nloc > 0 && nloc <= kMaxRecorders && s->ds.num_tris > 0;
+    if (automatic) {
+      use = use && work >= (uint64_t)s->ds.num_tris;
+      const int cap = (int)std::sqrt((double)kBatchMapCells / (6.0 * std::max(nloc, 1)));
+      res = std::max(8, std::min(res, cap / 32 * 32));
+    }
+    if (use) {
+      size_t free_b = 0, total_b = 0;
+      CU(cudaMemGetInfo(&free_b, &total_b));
+      const uint64_t fit = (uint64_t)(free_b / 2) / 32;
+      const uint64_t limit = std::min<uint64_t>(
+          automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
+      char msg[256] = "";
+      bool too_large = false;
+      CU(cudaEventRecord(b->ev0, st));
+      for (;;) {
+        const cudaError_t e = build_vis_map(s->ds, reinterpret_cast<const float(*)[3]>(locs.data()),
+                                            nloc, res, limit, st, &b->maps[i], &too_large, msg,
+                                            sizeof msg);
+        if (e != cudaSuccess)
+          return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
+                      "batch visibility map build (scene %zu): %s", i,
+                      msg[0] ? msg : cudaGetErrorString(e));
+        if (!too_large || !automatic || res <= 64) break;
+        res = std::max(64, (res * 3 / 4) / 32 * 32);
+      }
+      CU(cudaEventRecord(b->ev1, st));
+      CU(cudaEventSynchronize(b->ev1));
+      float ms = 0.0f;
+      CU(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+      b->map_build_ms += ms;
+      use = !too_large;
+    }
+    for (size_t r = 0; r < b->recs.size(); ++r)
+      if (b->jobs[(size_t)b->recs[r].job].scene == (int)i) b->recs[r].vis_index = use ? index[r] : -1;
+  }
+  if (recs_changed && !b->recs.empty())
+    CU(cudaMemcpy(b->d_recs, b->recs.data(), sizeof(DevRecorder) * b->recs.size(), cudaMemcpyHostToDevice));
+  return EAR_OK;
+}
+
+// Re-reads the scenes' device pointers (a BVH rebuild replaces them) and
+// their visibility maps; a change re-uploads the scene table and drops the
+// captured graph.
 ear_status sync_scenes(ear_batch* b) {
+  ear_status rc = build_batch_maps(b);
+  if (rc != EAR_OK) return rc;
   std::vector<SceneRef> now(b->scenes.size());
   for (size_t i = 0; i < b->scenes.size(); ++i) {
     if (!b->scenes[i]->bvh) return fail(EAR_ERR_STATE, "batch scene %zu has no LBVH", i);
-    now[i] = scene_ref(b->scenes[i], b->mat_base[i]);
+    now[i] = scene_ref(b->scenes[i], b->mat_base[i], b->maps[i]);
   }
   if (!b->h_scenes.empty() && std::memcmp(now.data(), b->h_scenes.data(), sizeof(SceneRef) * now.size()) == 0)
     return EAR_OK;
@@ -276,6 +375,8 @@ ear_status rebuild_scenes(ear_batch* b, int leaf) {
     o.box_pad = s->ds.box_pad;  // keep the padding the scene was built with
     o.max_leaf_size = leaf;
     o.builder = EAR_BVH_LBVH;
+    o.visibility_order = s->ds.any_order;
+    o.visibility_map = s->vis_opt;
     const ear_status rc = ear_scene_build_bvh(s, &o);
     if (rc != EAR_OK) return rc;
   }
@@ -522,6 +623,14 @@ ear_status ear_batch_run(ear_batch* b, ear_render_stats* stats) {
   float ms = 0.0f;
   CU(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
   fill_stats(cnt, b->a.num_items, ms, stats);
+  if (stats) {
+    stats->map_build_ms = b->map_build_ms;
+    for (const VisMap& m : b->maps) {
+      stats->map_bytes += m.bytes;
+      stats->map_res = std::max(stats->map_res, m.start ? m.res : 0);
+    }
+  }
+  b->map_build_ms = 0.0;
   b->ran = true;
   return EAR_OK;
 }
@@ -577,6 +686,7 @@ void ear_batch_destroy(ear_batch* b) {
   cudaFree(b->d_dvis);
   cudaFree(b->d_counters);
   cudaFree(b->d_err);
+  for (VisMap& m : b->maps) free_vis_map(&m);
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);

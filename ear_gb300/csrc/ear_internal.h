@@ -81,6 +81,7 @@ struct DevRecorder {
   int channels;
   int track0;  // first histogram track (global over a batch)
   int job;     // batch job the recorder belongs to (0 outside batches)
+  int vis_index;  // its list set in the scene's visibility maps (-1: none)
 };
 
 // One scene as the trace kernel addresses it.  A batch keeps a table of
@@ -98,6 +99,12 @@ struct __align__(16) SceneRef {
   int traverse_budget;
   int wide;     // 1: traverse nodes4, 0: nodes2
   int any_far;  // visibility tests visit the farthest hit child first
+  // listener visibility maps of the recorders (vis_res = 0: none); a cell
+  // holding more than vis_cap entries is left to the tree traversal
+  const uint32_t* vis_start;
+  const int2* vis_entries;
+  int vis_res;
+  int vis_cap;
 };
 
 // One (scene, source position, recorder set) of a batch.  Its work items
@@ -150,8 +157,7 @@ struct TraceArgs {
   int num_tracks;
   int2* first_last;  // [track][band]
   int* direct_vis;   // [recorder] direct-path visibility, or null
-  // listener visibility maps of the recorders (vis_res = 0: none); a cell
-  // holding more than vis_cap entries is left to the tree traversal
+  // listener visibility maps of a single render's recorders (as in SceneRef)
   const uint32_t* vis_start;
   const int2* vis_entries;
   int vis_res;

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "../../include/ear_gb300.h"
@@ -91,6 +92,16 @@ constexpr int64_t kWideFrom = 4096;
 void fill_stats(const unsigned long long* cnt, uint64_t num_items, double kernel_ms,
                 ear_render_stats* stats);
 
+// Visibility-map cells with more entries than this are left to the tree.
+constexpr int kVisWalkCap = 96;
+
+// Cells per face edge of the automatic visibility maps of a scene:
+// 4 sqrt(triangles), a multiple of 64 in [64, 2048].
+inline int vis_auto_res(int64_t num_tris) {
+  const double r = 4.0 * std::sqrt((double)num_tris);
+  return (int)std::min(2048.0, std::max(64.0, std::floor(r / 64.0) * 64.0));
+}
+
 }  // namespace ear
 
 struct ear_scene {
@@ -126,4 +137,5 @@ struct ear_scene {
   uint64_t vis_key = 0;
   bool vis_valid = false;   // `vis` (or vis_refused) belongs to vis_key
   bool vis_refused = false;  // the set's lists were above the entry limit
+  uint64_t bvh_gen = 0;       // counts ear_scene_build_bvh calls (leaf order changes)
 };

@@ -578,6 +578,10 @@ __device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef*
   S.mat_base = 0;
   S.num_mats = a.num_mats;
   S.traverse_budget = a.traverse_budget;
+  S.vis_start = a.vis_start;
+  S.vis_entries = a.vis_entries;
+  S.vis_res = a.vis_res;
+  S.vis_cap = a.vis_cap;
   return S;
 }
 
@@ -598,16 +602,15 @@ struct Vertex {
   bool conn;     // connect the recorders at this vertex
 };
 
-// Visibility test of the segment from `o` to recorder `ri` (sdir = its
-// location - o, len = |sdir|) through the recorder's visibility map: the
+// Visibility test of the segment from `o` to the recorder with list set
+// `ri` in the scene's maps (sdir = its location - o, len = |sdir|): the
 // entries of the cell of direction o - location nearer than the vertex, each
 // by the tree's own leaf test.  Returns 1 blocked, 0 clear, -1 when the map
 // leaves the test to the tree (degenerate direction, or a cell longer than
 // vis_cap).  The result equals the tree traversal's: the entries are every
 // triangle whose padded box meets the segment.
-__device__ __forceinline__ int vis_map_test(const TraceArgs& a, const SceneRef& S, int ri, V3 o,
-                                            V3 sdir, float len, Hit& h, LaneCounters& c,
-                                            int& err) {
+__device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 sdir, float len,
+                                            Hit& h, LaneCounters& c, int& err) {
   const float qx = -sdir.x, qy = -sdir.y, qz = -sdir.z;
   const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
   int f;
@@ -629,19 +632,19 @@ __device__ __forceinline__ int vis_map_test(const TraceArgs& a, const SceneRef& 
     v = qy;
   }
   if (!(m > 0.0f)) return -1;
-  const int res = a.vis_res;
+  const int res = S.vis_res;
   const uint32_t cell = ((uint32_t)(ri * 6 + f) * (uint32_t)res + (uint32_t)vis_cell(v / m, res)) *
                             (uint32_t)res +
                         (uint32_t)vis_cell(u / m, res);
-  const uint32_t b = __ldg(a.vis_start + cell), e = __ldg(a.vis_start + cell + 1);
-  if (e - b > (uint32_t)a.vis_cap) return -1;
+  const uint32_t b = __ldg(S.vis_start + cell), e = __ldg(S.vis_start + cell + 1);
+  if (e - b > (uint32_t)S.vis_cap) return -1;
   // entries are ordered by their boxes' distance from the recorder; a hit
   // point of the segment lies nearer than len (t > 1e-5)
   const float cut = len * 1.000244140625f;
   uint32_t i = b;
   bool blocked = false;
   for (; i < e; ++i) {
-    const int2 en = __ldg(a.vis_entries + i);
+    const int2 en = __ldg(S.vis_entries + i);
     if (__int_as_float(en.y) > cut) break;
     if (leaf_test<true>(S, ~en.x, o, sdir, h, c, err)) {
       blocked = true;
@@ -677,7 +680,8 @@ __device__ __forceinline__ int connect_one(const TraceArgs& a, const SceneRef* s
   const SceneRef S = scene_of<MODE>(a, s_scenes, st);
   const float slack = kSlackRel + S.box_pad / len;
   int vm = -1;
-  if (MODE != kModeBatch && a.vis_res > 0) vm = vis_map_test(a, S, ri, st.o, sdir, len, hh, c, err);
+  const int mi = MODE == kModeBatch ? R.vis_index : ri;
+  if (S.vis_res > 0 && mi >= 0) vm = vis_map_test(S, mi, st.o, sdir, len, hh, c, err);
   if (vm < 0) vm = traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err) ? 1 : 0;
   if (vm) return kBlockedSeg;
   if (!(dt > 0)) return kVisible;

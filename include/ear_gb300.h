@@ -128,9 +128,11 @@ typedef struct ear_bvh_opts {
      keep the traversal.  Built on a render's first use of a recorder set
      and kept until the set, the tree or this setting changes.  > 0: on,
      with this many cells per face edge (8..2048); -1: off; 0 = automatic:
-     on, with 4 sqrt(triangles) cells per edge (a multiple of 64,
-     64..2048), lowered while the lists would hold more than
-     EAR_VISMAP_AUTO_MAX_ENTRIES entries.  Never changes a result. */
+     built for renders of at least as many rays (times bands) as the scene
+     has triangles, with 4 sqrt(triangles) cells per edge (a multiple of
+     64, 64..2048), lowered while the lists would hold more than
+     EAR_VISMAP_AUTO_MAX_ENTRIES entries; used by any render while they
+     match its recorder set.  Never changes a result. */
   int32_t visibility_map;
   int32_t reserved;
 } ear_bvh_opts;

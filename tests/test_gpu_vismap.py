@@ -131,15 +131,21 @@ def test_fast_render_with_maps():
 
 
 def test_automatic_setting_and_rebuild():
-    """The automatic setting picks 4 sqrt(triangles) cells per face edge
-    (a multiple of 64, at least 64); a rebuilt tree or another recorder set
-    rebuilds the maps."""
+    """The automatic setting builds maps for renders of at least as many
+    paths as triangles, with 4 sqrt(triangles) cells per face edge (a
+    multiple of 64, at least 64), and lets shorter renders use them once
+    built; a rebuilt tree or another recorder set rebuilds them."""
     w = _crowded_room()
     kw = dict(w.render, num_rays=500)
+    short = dict(w.render, num_rays=100)  # 300 paths < 864 triangles
     with Tracer(w.vertices, w.material_ids, w.materials) as tr:
+        rs = tr.render(w.source, w.recorders, **short)
+        assert rs.stats["map_entries"] == 0 and rs.stats["map_res"] == 0
         r0 = tr.render(w.source, w.recorders, **kw)
         assert r0.stats["map_entries"] > 0 and r0.stats["map_res"] == 64
-        assert r0.stats["map_bytes"] > 0
+        assert r0.stats["map_bytes"] > 0 and r0.stats["map_build_ms"] > 0
+        rs = tr.render(w.source, w.recorders, **short)
+        assert rs.stats["map_entries"] > 0 and rs.stats["map_build_ms"] == 0
         tr.build_bvh(visibility_map=24)
         r1 = tr.render(w.source, w.recorders, **kw)
         assert r1.stats["map_build_ms"] > 0 and r1.stats["map_entries"] > 0
@@ -147,3 +153,34 @@ def test_automatic_setting_and_rebuild():
         assert r2.stats["map_build_ms"] > 0
         tr.build_bvh(visibility_map=-1)
         assert tr.render(w.source, w.recorders, **kw).stats["map_entries"] == 0
+
+
+def test_batch_with_maps_equals_plain_renders_without():
+    """A batch builds one map per scene over its jobs' distinct recorder
+    locations; its exact jobs count and record what plain renders without
+    maps do."""
+    from ear_gb300.batch import Batch, Job
+
+    w = _crowded_room()
+    render = dict(w.render, num_bins=44100)
+    src = np.asarray(w.source.location, np.float32)
+    sets = [w.recorders[:3], w.recorders[3:6], [w.recorders[6], w.recorders[0]], w.recorders[7:]]
+    jobs = [Job(scene=0, source=type(w.source)(location=src + np.float32(0.3 * k), gain=0.8),
+                recorders=rs, num_rays=700 + 100 * k, context=k) for k, rs in enumerate(sets)]
+    with Tracer(w.vertices, w.material_ids, w.materials, visibility_map=40) as on, \
+            Tracer(w.vertices, w.material_ids, w.materials, visibility_map=-1) as off:
+        plain = [off.render(j.source, j.recorders, exact=True,
+                            **dict(render, num_rays=j.num_rays, context=j.context)) for j in jobs]
+        b = Batch([on], jobs, exact=True, **{k: v for k, v in render.items() if k != "num_rays"})
+        st = b.run()
+        assert st["map_bytes"] > 0 and st["map_res"] == 40 and st["map_entries"] > 0
+        for k in ("segments", "shadow_queries", "contributions", "rays"):
+            assert int(st[k]) == sum(int(p.stats[k]) for p in plain), k
+        for i, p in enumerate(plain):
+            r = b.result(i)
+            np.testing.assert_array_equal(r.first_sample, p.first_sample)
+            np.testing.assert_array_equal(r.last_sample, p.last_sample)
+            e1 = (np.asarray(r.hist, np.float64) ** 2).sum(-1)
+            e2 = (np.asarray(p.hist, np.float64) ** 2).sum(-1)
+            assert (np.abs(e1 - e2) <= 1e-5 * np.maximum(e2, 1e-30)).all(), i
+        b.close()
