@@ -641,14 +641,35 @@ __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 
   // entries are ordered by their boxes' distance from the recorder; a hit
   // point of the segment lies nearer than len (t > 1e-5)
   const float cut = len * 1.000244140625f;
+  // two entries per step: both triangles' loads are in flight before the
+  // first test (Mesh::LineIntersection: 1e-5 < t < 1, src/Mesh.cpp:65)
   uint32_t i = b;
   bool blocked = false;
-  for (; i < e; ++i) {
-    const int2 en = __ldg(S.vis_entries + i);
-    if (__int_as_float(en.y) > cut) break;
-    if (leaf_test<true>(S, ~en.x, o, sdir, h, c, err)) {
+  while (i < e) {
+    const int2 e0 = __ldg(S.vis_entries + i);
+    const bool has1 = i + 1 < e;
+    const int2 e1 = has1 ? __ldg(S.vis_entries + i + 1) : e0;
+    if (__int_as_float(e0.y) > cut) break;
+    const bool use1 = has1 && __int_as_float(e1.y) <= cut;
+    const int p0 = clamp_index(e0.x, S.num_tris, err);
+    const int p1 = use1 ? clamp_index(e1.x, S.num_tris, err) : p0;
+    float4 A0, B0, A1, B1;
+    ldg256(S.tris + 4 * p0, A0, B0);
+    const float4 C0 = __ldg(S.tris + 4 * p0 + 2);
+    ldg256(S.tris + 4 * p1, A1, B1);
+    const float4 C1 = __ldg(S.tris + 4 * p1 + 2);
+    float t;
+    ++c.tris;
+    ++i;
+    if (mt_intersect(A0, B0, C0, o, sdir, t) && t > 1e-5f && t < 1.0f) {
       blocked = true;
-      ++i;
+      break;
+    }
+    if (!use1) break;
+    ++c.tris;
+    ++i;
+    if (mt_intersect(A1, B1, C1, o, sdir, t) && t > 1e-5f && t < 1.0f) {
+      blocked = true;
       break;
     }
   }
