@@ -124,15 +124,16 @@ typedef struct ear_bvh_opts {
      directions around it whose cells list the triangles (padded boxes) in
      their cone, nearest first.  A visibility test then runs the triangle
      test on its cell's entries nearer than the path vertex instead of
-     traversing the tree; cells longer than a limit, and batched renders,
-     keep the traversal.  Built on a render's first use of a recorder set
-     and kept until the set, the tree or this setting changes.  > 0: on,
-     with this many cells per face edge (8..2048); -1: off; 0 = automatic:
-     built for renders of at least as many rays (times bands) as the scene
-     has triangles, with 4 sqrt(triangles) cells per edge (a multiple of
-     64, 64..2048), lowered while the lists would hold more than
-     EAR_VISMAP_AUTO_MAX_ENTRIES entries; used by any render while they
-     match its recorder set.  Never changes a result. */
+     traversing the tree; cells longer than a limit keep the traversal.  A
+     render builds them on first use of a recorder set and keeps them until
+     the set, the tree or this setting changes; a batch builds one per scene
+     over its jobs' recorders.  > 0: on, with this many cells per face edge
+     (8..2048); -1: off; 0 = automatic: built for renders of at least as
+     many rays (times bands) as the scene has triangles, with
+     4 sqrt(triangles) cells per edge (a multiple of 64, 64..2048), lowered
+     while the lists would hold more than EAR_VISMAP_AUTO_MAX_ENTRIES
+     entries; used by any render while they match its recorder set.  Never
+     changes a result. */
   int32_t visibility_map;
   int32_t reserved;
 } ear_bvh_opts;
