@@ -597,10 +597,12 @@ def run_ours(args):
     per_launch = alg_bytes / args.steps
     # DRAM traffic of the trace kernel per launch, dram__bytes_read.sum +
     # dram__bytes_write.sum from one ncu capture of this default workload
-    # (1e7 rays/band, fast kernels); other workloads report null
+    # (1e7 rays/band, fast kernels, automatic visibility map); other
+    # workloads and settings report null
     traffic = None
-    if w.name == "relief-hall-20k-stereo" and int(kw["num_rays"]) == 10_000_000 and not exact:
-        traffic = 180_881_920
+    if (w.name == "relief-hall-20k-stereo" and int(kw["num_rays"]) == 10_000_000 and not exact
+            and args.vismap == 0):
+        traffic = 219_903_488
 
     # e2e through the C ABI from pinned host memory, every step
     e2e = None
