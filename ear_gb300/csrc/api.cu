@@ -475,14 +475,9 @@ ear_status choose_visibility_order(ear_scene* s, const ear_recorder* recs, int32
 // visibility_map): built on first use, reused while the set, the tree and
 // the setting stay the same.  A set whose lists would exceed the entry
 // limit keeps the tree traversal.  *build_ms receives the build time.
-ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t nrec, TraceArgs& a,
-                               cudaStream_t st, double* build_ms) {
-  *build_ms = 0.0;
-  a.vis_res = 0;
-  if (nrec <= 0 || s->vis_opt < 0 || s->ds.num_tris <= 0) return EAR_OK;
-  const bool automatic = s->vis_opt == 0;
-  int res = s->vis_opt;
-  if (automatic) res = vis_auto_res(s->ds.num_tris);
+// Identity of a recorder set's maps: the requested resolution, the tree
+// generation and the recorder locations (FNV-1a over their bits).
+uint64_t vis_map_key(const ear_scene* s, const ear_recorder* recs, int32_t nrec, int res) {
   uint64_t key = (1469598103934665603ull ^ (uint64_t)res) * 1099511628211ull;
   key = (key ^ s->bvh_gen) * 1099511628211ull;
   for (int32_t i = 0; i < nrec; ++i)
@@ -491,7 +486,25 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
       std::memcpy(&bits, &recs[i].location[k], sizeof bits);
       key = (key ^ bits) * 1099511628211ull;
     }
-  key = (key ^ (uint64_t)nrec) * 1099511628211ull;
+  return (key ^ (uint64_t)nrec) * 1099511628211ull;
+}
+
+void set_vis_args(const ear_scene* s, TraceArgs& a) {
+  a.vis_start = s->vis.start;
+  a.vis_entries = s->vis.entries;
+  a.vis_res = s->vis.res;
+  a.vis_cap = kVisWalkCap;
+}
+
+ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t nrec, TraceArgs& a,
+                               cudaStream_t st, double* build_ms) {
+  *build_ms = 0.0;
+  a.vis_res = 0;
+  if (nrec <= 0 || s->vis_opt < 0 || s->ds.num_tris <= 0) return EAR_OK;
+  const bool automatic = s->vis_opt == 0;
+  int res = s->vis_opt;
+  if (automatic) res = vis_auto_res(s->ds.num_tris);
+  const uint64_t key = vis_map_key(s, recs, nrec, res);
   if (!s->vis_valid || key != s->vis_key) {
     // automatic: a render of fewer paths than the scene has triangles
     // does not repay the build (a new recorder set per short render)
@@ -531,10 +544,7 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
     s->vis_valid = true;
   }
   if (s->vis_refused) return EAR_OK;
-  a.vis_start = s->vis.start;
-  a.vis_entries = s->vis.entries;
-  a.vis_res = s->vis.res;
-  a.vis_cap = kVisWalkCap;
+  set_vis_args(s, a);
   return EAR_OK;
 }
 
@@ -1147,6 +1157,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     d.channels = r.channels;
     d.track0 = tracks;
     d.job = 0;
+    d.vis_index = i;
     tracks += r.channels;
   }
   CU(cudaSetDevice(s->device));
@@ -1196,6 +1207,12 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.error_flag = reinterpret_cast<int*>(scratch + kNaError);
   a.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
   a.dbg_band = -1;
+  // listener visibility maps an earlier ear_render built for this recorder
+  // set are read; none is built here (a build allocates)
+  if (nrec > 0 && s->vis_opt >= 0 && s->vis_valid && !s->vis_refused && s->vis.start) {
+    const int res = s->vis_opt > 0 ? s->vis_opt : vis_auto_res(s->ds.num_tris);
+    if (vis_map_key(s, recs, nrec, res) == s->vis_key) set_vis_args(s, a);
+  }
 
   cudaStream_t st = (cudaStream_t)p->stream;
   const int rows = tracks * 3;
@@ -1262,11 +1279,9 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     stats->triangle_tests = cnt[kTriTests];
     stats->splat_bins = cnt[kSplatBins];
     stats->kernel_ms = ms;
-    stats->map_entries = 0;  // the no-alloc path keeps the tree traversal
+    stats->map_entries = cnt[kMapEntries];
     stats->map_build_ms = 0.0;
-    stats->map_bytes = 0;
-    stats->map_res = 0;
-    stats->reserved1 = 0;
+    map_stats(s, a, stats);
   }
   return EAR_OK;
 }

@@ -428,7 +428,10 @@ ear_status ear_batch_tune(ear_batch* batch, const ear_tune_opts* opts, ear_tune_
    - The array is shared by every call on the device and keeps the last
      call's contents (each call clears what must start at zero).  Calls
      whose GPU work overlaps -- e.g. on two streams -- race on it: serialise
-     them. */
+     them.
+   - Listener visibility maps (ear_bvh_opts.visibility_map) are read when
+     an earlier ear_render built them for the same recorder set, never
+     built here: render once with ear_render before going real-time. */
 ear_status ear_render_noalloc(ear_scene* scene, const ear_source* source,
                               const ear_recorder* recorders,
                               int32_t num_recorders,

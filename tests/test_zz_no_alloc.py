@@ -55,6 +55,29 @@ def test_noalloc_matches_render_twice(exact):
             np.testing.assert_array_equal(last, ref.last_sample)
             for key in ("rays", "segments", "shadow_queries", "contributions"):
                 assert stats[key] == ref.stats[key], key
+            # the visibility maps ear_render built are read, not rebuilt
+            assert stats["map_res"] == ref.stats["map_res"] > 0
+            assert stats["map_entries"] == ref.stats["map_entries"]
+            assert stats["map_build_ms"] == 0.0
+
+
+def test_noalloc_without_maps_traverses_the_tree():
+    """With no map built for the recorder set, the no-alloc render builds
+    none and matches ear_render without maps."""
+    torch = pytest.importorskip("torch")
+    w = scenes.small_test_room()
+    kw = dict(w.render)
+    kw["num_rays"] = 2000
+    with Tracer(w.vertices, w.material_ids, w.materials, device=0, visibility_map=-1) as tr:
+        ref = tr.render(w.source, w.recorders, exact=True, **kw)
+        params = make_params(exact=True, **kw)
+        out = torch.empty((w.num_tracks, 3, kw["num_bins"]), dtype=torch.float32, device="cuda")
+        rc, first, last, stats = _noalloc(tr, w, params, out)
+        assert rc == N.EAR_OK, N.lib().ear_last_error()
+        assert stats["map_entries"] == 0 and stats["map_res"] == 0
+        for key in ("rays", "segments", "shadow_queries", "contributions"):
+            assert stats[key] == ref.stats[key], key
+        np.testing.assert_array_equal(first, ref.first_sample)
 
 
 def test_noalloc_rejects_requests_beyond_its_scratch():
