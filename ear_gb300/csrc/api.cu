@@ -528,6 +528,12 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
     for (;;) {
       const cudaError_t e = build_vis_map(s->ds, locs, nrec, res, limit, st, &s->vis, &too_large,
                                           msg, sizeof msg);
+      if (e == cudaErrorMemoryAllocation && automatic) {
+        // the automatic maps are an accelerator: without room the tree serves
+        cudaGetLastError();
+        too_large = true;
+        break;
+      }
       if (e != cudaSuccess)
         return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
                     "visibility map build: %s", msg[0] ? msg : cudaGetErrorString(e));

@@ -174,6 +174,12 @@ ear_status build_batch_maps(ear_batch* b) {
         const cudaError_t e = build_vis_map(s->ds, reinterpret_cast<const float(*)[3]>(locs.data()),
                                             nloc, res, limit, st, &b->maps[i], &too_large, msg,
                                             sizeof msg);
+        if (e == cudaErrorMemoryAllocation && automatic) {
+          // the automatic maps are an accelerator: without room the tree serves
+          cudaGetLastError();
+          too_large = true;
+          break;
+        }
         if (e != cudaSuccess)
           return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
                       "batch visibility map build (scene %zu): %s", i,
