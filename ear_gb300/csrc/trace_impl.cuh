@@ -610,7 +610,7 @@ struct Vertex {
 // vis_cap).  The result equals the tree traversal's: the entries are every
 // triangle whose padded box meets the segment.
 __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 sdir, float len,
-                                            Hit& h, LaneCounters& c, int& err) {
+                                            LaneCounters& c, int& err) {
   const float qx = -sdir.x, qy = -sdir.y, qz = -sdir.z;
   const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
   int f;
@@ -702,7 +702,7 @@ __device__ __forceinline__ int connect_one(const TraceArgs& a, const SceneRef* s
   const float slack = kSlackRel + S.box_pad / len;
   int vm = -1;
   const int mi = MODE == kModeBatch ? R.vis_index : ri;
-  if (S.vis_res > 0 && mi >= 0) vm = vis_map_test(S, mi, st.o, sdir, len, hh, c, err);
+  if (S.vis_res > 0 && mi >= 0) vm = vis_map_test(S, mi, st.o, sdir, len, c, err);
   if (vm < 0) vm = traverse<true>(S, st.o, sdir, 1.0f, slack, hh, c, err) ? 1 : 0;
   if (vm) return kBlockedSeg;
   if (!(dt > 0)) return kVisible;
