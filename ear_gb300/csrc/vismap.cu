@@ -29,6 +29,8 @@
 // Compiled with --fmad=false: the count and fill passes must compute the
 // same cells.
 
+#include <cub/block/block_reduce.cuh>
+#include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -185,12 +187,34 @@ __device__ __forceinline__ bool cell_meets(const TriProj& tp, int iu, int iv, in
   return true;
 }
 
-__global__ void k_vis_count(const VisBuildArgs a, uint64_t* __restrict__ count) {
+// (recorder, triangle) items whose cell rectangles cover more than this
+// many cells -- large triangles close to a recorder -- are counted and
+// filled by a whole block each (k_vis_count_big, k_vis_fill_big), in the
+// same cell order as one thread would.
+constexpr uint64_t kVisBigItem = 1024;
+constexpr int kVisBigBlock = 256;
+
+__device__ __forceinline__ uint64_t rect_cells(const float* lo, const float* hi, int res) {
+  uint64_t n = 0;
+  for (int f = 0; f < 6; ++f) {
+    FaceRect r;
+    if (face_rect(lo, hi, f, res, r)) n += (uint64_t)(r.u1 - r.u0 + 1) * (uint64_t)(r.v1 - r.v0 + 1);
+  }
+  return n;
+}
+
+__global__ void k_vis_count(const VisBuildArgs a, uint64_t* __restrict__ count,
+                            int64_t* __restrict__ big, unsigned long long* __restrict__ num_big) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)a.nrec * a.num_tris) return;
   const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
   float lo[3], hi[3], t[3][3];
   rel_box(a, ri, pos, lo, hi, t);
+  if (rect_cells(lo, hi, a.res) > kVisBigItem) {
+    big[atomicAdd(num_big, 1ull)] = i;
+    count[i] = 0;  // k_vis_count_big
+    return;
+  }
   uint64_t n = 0;
   for (int f = 0; f < 6; ++f) {
     FaceRect r;
@@ -206,6 +230,75 @@ __global__ void k_vis_count(const VisBuildArgs a, uint64_t* __restrict__ count) 
   count[i] = n;
 }
 
+__global__ void __launch_bounds__(kVisBigBlock) k_vis_count_big(const VisBuildArgs a,
+                                                                const int64_t* __restrict__ big,
+                                                                uint64_t* __restrict__ count) {
+  using Reduce = cub::BlockReduce<unsigned long long, kVisBigBlock>;
+  __shared__ typename Reduce::TempStorage tmp;
+  const int64_t i = big[blockIdx.x];
+  const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
+  float lo[3], hi[3], t[3][3];
+  rel_box(a, ri, pos, lo, hi, t);
+  unsigned long long n = 0;
+  for (int f = 0; f < 6; ++f) {
+    FaceRect r;
+    if (!face_rect(lo, hi, f, a.res, r)) continue;
+    TriProj tp;
+    const bool tri = tri_proj(t, f, a.pad, tp);
+    const int64_t w = r.u1 - r.u0 + 1, area = w * (int64_t)(r.v1 - r.v0 + 1);
+    for (int64_t k = threadIdx.x; k < area; k += kVisBigBlock) {
+      const int u = r.u0 + (int)(k % w), v = r.v0 + (int)(k / w);
+      n += (!tri || cell_meets(tp, u, v, a.res)) ? 1u : 0u;
+    }
+  }
+  const unsigned long long total = Reduce(tmp).Sum(n);
+  if (threadIdx.x == 0) count[i] = total;
+}
+
+__global__ void __launch_bounds__(kVisBigBlock) k_vis_fill_big(const VisBuildArgs a,
+                                                               const int64_t* __restrict__ big,
+                                                               const uint64_t* __restrict__ count,
+                                                               const uint64_t* __restrict__ offset,
+                                                               uint64_t* __restrict__ keys,
+                                                               int32_t* __restrict__ vals) {
+  using Scan = cub::BlockScan<unsigned, kVisBigBlock>;
+  __shared__ typename Scan::TempStorage tmp;
+  const int64_t i = big[blockIdx.x];
+  const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
+  float lo[3], hi[3], t[3][3];
+  const float dist = rel_box(a, ri, pos, lo, hi, t);
+  const uint64_t cells_per_rec = 6ull * a.res * a.res;
+  const uint64_t n = count[i], o = offset[i];
+  const uint64_t dbits = __float_as_uint(dist);
+  uint64_t w = 0;  // entries written so far (uniform over the block)
+  for (int f = 0; f < 6; ++f) {
+    FaceRect r;
+    if (!face_rect(lo, hi, f, a.res, r)) continue;
+    TriProj tp;
+    const bool tri = tri_proj(t, f, a.pad, tp);
+    const int64_t rw = r.u1 - r.u0 + 1, area = rw * (int64_t)(r.v1 - r.v0 + 1);
+    for (int64_t base = 0; base < area; base += kVisBigBlock) {
+      const int64_t k = base + threadIdx.x;
+      const int u = r.u0 + (int)(k % rw), v = r.v0 + (int)(k / rw);
+      const unsigned in = (k < area && (!tri || cell_meets(tp, u, v, a.res))) ? 1u : 0u;
+      unsigned at = 0, chunk = 0;
+      Scan(tmp).ExclusiveSum(in, at, chunk);
+      __syncthreads();  // tmp is reused by the next chunk
+      if (in && w + at < n) {
+        const uint64_t cell = ri * cells_per_rec + ((uint64_t)f * a.res + v) * a.res + u;
+        keys[o + w + at] = (cell << 32) | dbits;
+        vals[o + w + at] = pos;
+      }
+      w += chunk;
+    }
+  }
+  // never reached with --fmad=false (both passes compute the same cells)
+  for (uint64_t k = w + threadIdx.x; k < n; k += kVisBigBlock) {
+    keys[o + k] = ((uint64_t)a.nrec * cells_per_rec) << 32;
+    vals[o + k] = 0;
+  }
+}
+
 __global__ void k_vis_fill(const VisBuildArgs a, const uint64_t* __restrict__ count,
                            const uint64_t* __restrict__ offset, uint64_t* __restrict__ keys,
                            int32_t* __restrict__ vals) {
@@ -214,6 +307,7 @@ __global__ void k_vis_fill(const VisBuildArgs a, const uint64_t* __restrict__ co
   const int ri = (int)(i / a.num_tris), pos = (int)(i % a.num_tris);
   float lo[3], hi[3], t[3][3];
   const float dist = rel_box(a, ri, pos, lo, hi, t);
+  if (rect_cells(lo, hi, a.res) > kVisBigItem) return;  // k_vis_fill_big
   const uint64_t cells_per_rec = 6ull * a.res * a.res;
   const uint64_t n = count[i];
   uint64_t o = offset[i], w = 0;
@@ -296,6 +390,9 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
   VisBuildArgs a = {};
   uint64_t *count = nullptr, *offset = nullptr, *keys = nullptr, *keys2 = nullptr;
   int32_t *vals = nullptr, *vals2 = nullptr;
+  int64_t* big = nullptr;
+  unsigned long long* d_num_big = nullptr;
+  unsigned long long num_big = 0;
   void* tmp = nullptr;
   size_t tmp_bytes = 0, need = 0;
   uint64_t total = 0, last_count = 0;
@@ -318,9 +415,18 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
   {
     VCK(cudaMalloc(&count, sizeof(uint64_t) * items));
     VCK(cudaMalloc(&offset, sizeof(uint64_t) * items));
+    VCK(cudaMalloc(&big, sizeof(int64_t) * items));
+    VCK(cudaMalloc(&d_num_big, sizeof(unsigned long long)));
+    VCK(cudaMemsetAsync(d_num_big, 0, sizeof(unsigned long long), st));
     const unsigned g = (unsigned)((items + B - 1) / B);
-    k_vis_count<<<g, B, 0, st>>>(a, count);
+    k_vis_count<<<g, B, 0, st>>>(a, count, big, d_num_big);
     VCK(cudaGetLastError());
+    VCK(cudaMemcpyAsync(&num_big, d_num_big, sizeof num_big, cudaMemcpyDeviceToHost, st));
+    VCK(cudaStreamSynchronize(st));
+    if (num_big > 0) {
+      k_vis_count_big<<<(unsigned)num_big, kVisBigBlock, 0, st>>>(a, big, count);
+      VCK(cudaGetLastError());
+    }
     VCK(cub::DeviceScan::ExclusiveSum(nullptr, need, count, offset, items, st));
     VCK(cudaMalloc(&tmp, need));
     tmp_bytes = need;
@@ -344,6 +450,10 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
     VCK(cudaMalloc(&vals2, sizeof(int32_t) * std::max<int64_t>(n, 1)));
     k_vis_fill<<<g, B, 0, st>>>(a, count, offset, keys, vals);
     VCK(cudaGetLastError());
+    if (num_big > 0) {
+      k_vis_fill_big<<<(unsigned)num_big, kVisBigBlock, 0, st>>>(a, big, count, offset, keys, vals);
+      VCK(cudaGetLastError());
+    }
     cub::DoubleBuffer<uint64_t> dk(keys, keys2);
     cub::DoubleBuffer<int32_t> dv(vals, vals2);
     const int end_bit = 32 + bits_for(cells);
@@ -369,6 +479,8 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
 done:
   cudaFree(count);
   cudaFree(offset);
+  cudaFree(big);
+  cudaFree(d_num_big);
   cudaFree(keys);
   cudaFree(keys2);
   cudaFree(vals);
