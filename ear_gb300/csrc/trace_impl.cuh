@@ -33,6 +33,7 @@
 
 #include "ear_internal.h"
 #include "ear_record.cuh"
+#include "vismap_geom.h"
 
 namespace ear {
 namespace EAR_NS {
@@ -611,36 +612,16 @@ struct Vertex {
 // triangle whose padded box meets the segment.
 __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 sdir, float len,
                                             LaneCounters& c, int& err) {
-  const float qx = -sdir.x, qy = -sdir.y, qz = -sdir.z;
-  const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
-  int f;
-  float m, u, v;
-  if (ax >= ay && ax >= az) {
-    f = qx > 0.0f ? 0 : 1;
-    m = ax;
-    u = qy;
-    v = qz;
-  } else if (ay >= az) {
-    f = qy > 0.0f ? 2 : 3;
-    m = ay;
-    u = qx;
-    v = qz;
-  } else {
-    f = qz > 0.0f ? 4 : 5;
-    m = az;
-    u = qx;
-    v = qy;
-  }
-  if (!(m > 0.0f)) return -1;
+  int f, iu, iv;
   const int res = S.vis_res;
-  const uint32_t cell = ((uint32_t)(ri * 6 + f) * (uint32_t)res + (uint32_t)vis_cell(v / m, res)) *
-                            (uint32_t)res +
-                        (uint32_t)vis_cell(u / m, res);
+  if (!vis_query_cell(sdir.x, sdir.y, sdir.z, res, f, iu, iv)) return -1;
+  const uint32_t cell =
+      ((uint32_t)(ri * 6 + f) * (uint32_t)res + (uint32_t)iv) * (uint32_t)res + (uint32_t)iu;
   const uint32_t b = __ldg(S.vis_start + cell), e = __ldg(S.vis_start + cell + 1);
   if (e - b > (uint32_t)S.vis_cap) return -1;
   // entries are ordered by their boxes' distance from the recorder; a hit
   // point of the segment lies nearer than len (t > 1e-5)
-  const float cut = len * 1.000244140625f;
+  const float cut = vis_cut(len);
   // two entries per step: both triangles' loads are in flight before the
   // first test (Mesh::LineIntersection: 1e-5 < t < 1, src/Mesh.cpp:65)
   uint32_t i = b;

@@ -12,19 +12,8 @@
 // its root.
 //
 // The lists are conservative, so the result is the tree traversal's bit
-// for bit: the traversal already relies on every point where the triangle
-// test can report a hit lying inside the triangle's box padded by box_pad;
-// here the boxes are padded by 2 box_pad, which also covers the rounding
-// of the segment's direction.  A box's cells are bounded in closed form:
-// over a box's points with major coordinate a in (max(a0, 0), a1] and
-// minor coordinate y in [y0, y1] the ratio y / a ranges from y0 / a1 (y0 >=
-// 0) or y0 / max(a0, 0) (y0 < 0) to y1 / a1 (y1 <= 0) or y1 / max(a0, 0)
-// (y1 > 0), unbounded where max(a0, 0) = 0.  Both the bounds and the
-// queries go through vis_cell(), which is monotonic, with a relative margin
-// of 2e-6 on the bounds against the rounding of the divisions.  Where a
-// triangle lies wholly in front of a face, its cells are further limited
-// to those meeting its projection widened by the padding's angular size
-// (tri_proj, cell_meets).
+// for bit; the geometry that makes them so (cells of a padded box, of a
+// projected triangle, of a query direction) is in vismap_geom.h.
 //
 // Compiled with --fmad=false: the count and fill passes must compute the
 // same cells.
@@ -39,6 +28,7 @@
 #include <algorithm>
 
 #include "ear_internal.h"
+#include "vismap_geom.h"
 
 namespace ear {
 namespace {
@@ -53,138 +43,16 @@ struct VisBuildArgs {
   int num_tris;
 };
 
-struct FaceRect {
-  int u0, u1, v0, v1;
-};
-
-__device__ __forceinline__ void ratio_range(float y0, float y1, float xa, float a1, float& lo,
-                                            float& hi) {
-  lo = y0 >= 0.0f ? y0 / a1 : (xa > 0.0f ? y0 / xa : -INFINITY);
-  hi = y1 <= 0.0f ? y1 / a1 : (xa > 0.0f ? y1 / xa : INFINITY);
-  lo -= 2e-6f + 2e-6f * fabsf(lo);
-  hi += 2e-6f + 2e-6f * fabsf(hi);
-  lo = fmaxf(lo, -1.0f);
-  hi = fminf(hi, 1.0f);
-}
-
-// Cells of face f met by the box [lo, hi] (coordinates relative to the
-// recorder).  Faces: 2 * axis + (negative side).
-__device__ __forceinline__ bool face_rect(const float* lo, const float* hi, int f, int res,
-                                          FaceRect& r) {
-  const int m = f >> 1;
-  const bool neg = f & 1;
-  const float a0 = neg ? -hi[m] : lo[m];
-  const float a1 = neg ? -lo[m] : hi[m];
-  if (!(a1 > 0.0f)) return false;
-  const float xa = fmaxf(a0, 0.0f);
-  const int p = m == 0 ? 1 : 0;
-  const int q = m == 2 ? 1 : 2;
-  float ulo, uhi, vlo, vhi;
-  ratio_range(lo[p], hi[p], xa, a1, ulo, uhi);
-  ratio_range(lo[q], hi[q], xa, a1, vlo, vhi);
-  if (!(ulo <= uhi) || !(vlo <= vhi)) return false;
-  r.u0 = vis_cell(ulo, res);
-  r.u1 = vis_cell(uhi, res);
-  r.v0 = vis_cell(vlo, res);
-  r.v1 = vis_cell(vhi, res);
-  return true;
-}
-
 // Padded box of the triangle at leaf position `pos`, relative to recorder
 // `ri`, its distance from the recorder (rounded down) and the relative
 // vertices t[3][3].
 __device__ __forceinline__ float rel_box(const VisBuildArgs& a, int ri, int pos, float* lo,
                                          float* hi, float (*t)[3]) {
   const int orig = __float_as_int(__ldg(&a.tris[4 * (size_t)pos].w));
-  const float* v = a.verts + 9 * (size_t)orig;
-  float d2 = 0.0f;
-  for (int k = 0; k < 3; ++k) {
-    const float x0 = __ldg(v + k), x1 = __ldg(v + 3 + k), x2 = __ldg(v + 6 + k);
-    lo[k] = (fminf(fminf(x0, x1), x2) - a.pad) - a.loc[ri][k];
-    hi[k] = (fmaxf(fmaxf(x0, x1), x2) + a.pad) - a.loc[ri][k];
-    t[0][k] = x0 - a.loc[ri][k];
-    t[1][k] = x1 - a.loc[ri][k];
-    t[2][k] = x2 - a.loc[ri][k];
-    const float g = fmaxf(fmaxf(lo[k], -hi[k]), 0.0f);
-    d2 += g * g;
-  }
-  return sqrtf(d2) * 0.99999f;
-}
-
-// The triangle seen from the recorder on face f: where all three vertices
-// lie beyond the padding in front of the face, the directions of the
-// padded triangle T + [-P, P]^3 fall inside the projected triangle
-// (u_i, v_i) = (y_i, z_i) / a_i widened by du = P (1 + max |u_i|) /
-// (min a_i - P) (and dv alike): u(t + d) - u(t) = (d_y - u(t) d_a) /
-// (t_a + d_a).  P carries a tenth more for the rounding of the relative
-// vertices, the widths 1e-5 more for the divisions.
-struct TriProj {
-  float u[3], v[3];
-  float du, dv;
-  float umin, umax, vmin, vmax;
-  float eps;  // bound on the rounding of u_i, v_i (relative 1e-6 of the largest)
-};
-
-__device__ __forceinline__ bool tri_proj(const float (*t)[3], int f, float pad, TriProj& tp) {
-  const int m = f >> 1;
-  const bool neg = f & 1;
-  const int p = m == 0 ? 1 : 0;
-  const int q = m == 2 ? 1 : 2;
-  const float P = pad * 1.1f;
-  float amin = INFINITY, mu = 0.0f, mv = 0.0f;
-  float ai[3];
-  for (int i = 0; i < 3; ++i) {
-    ai[i] = neg ? -t[i][m] : t[i][m];
-    amin = fminf(amin, ai[i]);
-  }
-  if (!(amin > 2.0f * P)) return false;
-  tp.umin = tp.vmin = INFINITY;
-  tp.umax = tp.vmax = -INFINITY;
-  for (int i = 0; i < 3; ++i) {
-    tp.u[i] = t[i][p] / ai[i];
-    tp.v[i] = t[i][q] / ai[i];
-    mu = fmaxf(mu, fabsf(tp.u[i]));
-    mv = fmaxf(mv, fabsf(tp.v[i]));
-    tp.umin = fminf(tp.umin, tp.u[i]);
-    tp.umax = fmaxf(tp.umax, tp.u[i]);
-    tp.vmin = fminf(tp.vmin, tp.v[i]);
-    tp.vmax = fmaxf(tp.vmax, tp.v[i]);
-  }
-  const float den = amin - P;
-  tp.du = P * (1.0f + mu) / den * 1.0001f + 1e-5f;
-  tp.dv = P * (1.0f + mv) / den * 1.0001f + 1e-5f;
-  tp.eps = 1e-6f * (1.0f + fmaxf(mu, mv));
-  return true;
-}
-
-// Does cell (iu, iv) meet the widened projected triangle?  Separating axes:
-// the cell's own (the triangle's bounding box) and the three edge normals.
-// An edge function n . (c - P_i) moves by at most 2 eps (|c - P_i| + |P_j -
-// P_i|) when the vertices move by eps, so a corner separates only beyond
-// that (plus the products' rounding); an edge whose orientation the same
-// bound leaves open (a sliver seen edge-on) never separates.
-__device__ __forceinline__ bool cell_meets(const TriProj& tp, int iu, int iv, int res) {
-  const float w = 2.0f / (float)res;
-  const float x0 = (-1.0f + (float)iu * w) - tp.du, x1 = (-1.0f + (float)(iu + 1) * w) + tp.du;
-  const float y0 = (-1.0f + (float)iv * w) - tp.dv, y1 = (-1.0f + (float)(iv + 1) * w) + tp.dv;
-  if (x1 < tp.umin || x0 > tp.umax || y1 < tp.vmin || y0 > tp.vmax) return false;
-  for (int e = 0; e < 3; ++e) {
-    const int i = e, j = e == 2 ? 0 : e + 1, k = e == 0 ? 2 : e - 1;
-    float nx = -(tp.v[j] - tp.v[i]), ny = tp.u[j] - tp.u[i];
-    const float len = fabsf(nx) + fabsf(ny);
-    const float dk = fabsf(tp.u[k] - tp.u[i]) + fabsf(tp.v[k] - tp.v[i]);
-    const float side = nx * (tp.u[k] - tp.u[i]) + ny * (tp.v[k] - tp.v[i]);
-    if (!(fabsf(side) > 2.0f * tp.eps * (dk + len) + 1e-6f * len * dk)) continue;
-    if (side < 0.0f) {
-      nx = -nx;
-      ny = -ny;
-    }
-    const float cu = nx > 0.0f ? x1 : x0, cv = ny > 0.0f ? y1 : y0;
-    const float reach = nx * (cu - tp.u[i]) + ny * (cv - tp.v[i]);
-    const float dc = fabsf(cu - tp.u[i]) + fabsf(cv - tp.v[i]);
-    if (reach < -(2.0f * tp.eps * (dc + len) + 1e-6f * len * dc)) return false;
-  }
-  return true;
+  const float* src = a.verts + 9 * (size_t)orig;
+  float v[9];
+  for (int k = 0; k < 9; ++k) v[k] = __ldg(src + k);
+  return vis_rel_box(v, a.loc[ri], a.pad, lo, hi, t);
 }
 
 // (recorder, triangle) items whose cell rectangles cover more than this
@@ -197,8 +65,8 @@ constexpr int kVisBigBlock = 256;
 __device__ __forceinline__ uint64_t rect_cells(const float* lo, const float* hi, int res) {
   uint64_t n = 0;
   for (int f = 0; f < 6; ++f) {
-    FaceRect r;
-    if (face_rect(lo, hi, f, res, r)) n += (uint64_t)(r.u1 - r.u0 + 1) * (uint64_t)(r.v1 - r.v0 + 1);
+    VisFaceRect r;
+    if (vis_face_rect(lo, hi, f, res, r)) n += (uint64_t)(r.u1 - r.u0 + 1) * (uint64_t)(r.v1 - r.v0 + 1);
   }
   return n;
 }
@@ -217,15 +85,15 @@ __global__ void k_vis_count(const VisBuildArgs a, uint64_t* __restrict__ count,
   }
   uint64_t n = 0;
   for (int f = 0; f < 6; ++f) {
-    FaceRect r;
-    if (!face_rect(lo, hi, f, a.res, r)) continue;
-    TriProj tp;
-    if (!tri_proj(t, f, a.pad, tp)) {
+    VisFaceRect r;
+    if (!vis_face_rect(lo, hi, f, a.res, r)) continue;
+    VisTriProj tp;
+    if (!vis_tri_proj(t, f, a.pad, tp)) {
       n += (uint64_t)(r.u1 - r.u0 + 1) * (uint64_t)(r.v1 - r.v0 + 1);
       continue;
     }
     for (int v = r.v0; v <= r.v1; ++v)
-      for (int u = r.u0; u <= r.u1; ++u) n += cell_meets(tp, u, v, a.res) ? 1u : 0u;
+      for (int u = r.u0; u <= r.u1; ++u) n += vis_cell_meets(tp, u, v, a.res) ? 1u : 0u;
   }
   count[i] = n;
 }
@@ -241,14 +109,14 @@ __global__ void __launch_bounds__(kVisBigBlock) k_vis_count_big(const VisBuildAr
   rel_box(a, ri, pos, lo, hi, t);
   unsigned long long n = 0;
   for (int f = 0; f < 6; ++f) {
-    FaceRect r;
-    if (!face_rect(lo, hi, f, a.res, r)) continue;
-    TriProj tp;
-    const bool tri = tri_proj(t, f, a.pad, tp);
+    VisFaceRect r;
+    if (!vis_face_rect(lo, hi, f, a.res, r)) continue;
+    VisTriProj tp;
+    const bool tri = vis_tri_proj(t, f, a.pad, tp);
     const int64_t w = r.u1 - r.u0 + 1, area = w * (int64_t)(r.v1 - r.v0 + 1);
     for (int64_t k = threadIdx.x; k < area; k += kVisBigBlock) {
       const int u = r.u0 + (int)(k % w), v = r.v0 + (int)(k / w);
-      n += (!tri || cell_meets(tp, u, v, a.res)) ? 1u : 0u;
+      n += (!tri || vis_cell_meets(tp, u, v, a.res)) ? 1u : 0u;
     }
   }
   const unsigned long long total = Reduce(tmp).Sum(n);
@@ -272,15 +140,15 @@ __global__ void __launch_bounds__(kVisBigBlock) k_vis_fill_big(const VisBuildArg
   const uint64_t dbits = __float_as_uint(dist);
   uint64_t w = 0;  // entries written so far (uniform over the block)
   for (int f = 0; f < 6; ++f) {
-    FaceRect r;
-    if (!face_rect(lo, hi, f, a.res, r)) continue;
-    TriProj tp;
-    const bool tri = tri_proj(t, f, a.pad, tp);
+    VisFaceRect r;
+    if (!vis_face_rect(lo, hi, f, a.res, r)) continue;
+    VisTriProj tp;
+    const bool tri = vis_tri_proj(t, f, a.pad, tp);
     const int64_t rw = r.u1 - r.u0 + 1, area = rw * (int64_t)(r.v1 - r.v0 + 1);
     for (int64_t base = 0; base < area; base += kVisBigBlock) {
       const int64_t k = base + threadIdx.x;
       const int u = r.u0 + (int)(k % rw), v = r.v0 + (int)(k / rw);
-      const unsigned in = (k < area && (!tri || cell_meets(tp, u, v, a.res))) ? 1u : 0u;
+      const unsigned in = (k < area && (!tri || vis_cell_meets(tp, u, v, a.res))) ? 1u : 0u;
       unsigned at = 0, chunk = 0;
       Scan(tmp).ExclusiveSum(in, at, chunk);
       __syncthreads();  // tmp is reused by the next chunk
@@ -313,13 +181,13 @@ __global__ void k_vis_fill(const VisBuildArgs a, const uint64_t* __restrict__ co
   uint64_t o = offset[i], w = 0;
   const uint64_t dbits = __float_as_uint(dist);
   for (int f = 0; f < 6; ++f) {
-    FaceRect r;
-    if (!face_rect(lo, hi, f, a.res, r)) continue;
-    TriProj tp;
-    const bool tri = tri_proj(t, f, a.pad, tp);
+    VisFaceRect r;
+    if (!vis_face_rect(lo, hi, f, a.res, r)) continue;
+    VisTriProj tp;
+    const bool tri = vis_tri_proj(t, f, a.pad, tp);
     for (int v = r.v0; v <= r.v1; ++v)
       for (int u = r.u0; u <= r.u1 && w < n; ++u) {
-        if (tri && !cell_meets(tp, u, v, a.res)) continue;
+        if (tri && !vis_cell_meets(tp, u, v, a.res)) continue;
         const uint64_t cell = ri * cells_per_rec + ((uint64_t)f * a.res + v) * a.res + u;
         keys[o + w] = (cell << 32) | dbits;
         vals[o + w] = pos;
