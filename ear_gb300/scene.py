@@ -350,9 +350,10 @@ class Scene:
     """Mirror of the reference's Scene (src/Scene.h:42-79) over the GPU
     tracer.  Meshes are (n, 9) triangle arrays tagged with a material name."""
 
-    def __init__(self, device: int = 0, box_pad: float = -1.0):
+    def __init__(self, device: int = 0, box_pad: float = -1.0, visibility_map: int = 0):
         self.device = device
         self.box_pad = box_pad
+        self.visibility_map = visibility_map
         self.meshes: list[tuple[np.ndarray, str]] = []
         self.materials: dict[str, Material] = {}
         self.listeners: list[Recorder] = []
@@ -388,7 +389,8 @@ class Scene:
     def tracer(self) -> Tracer:
         if self._tracer is None:
             v, ids, mats = self.geometry()
-            self._tracer = Tracer(v, ids, mats, device=self.device, box_pad=self.box_pad)
+            self._tracer = Tracer(v, ids, mats, device=self.device, box_pad=self.box_pad,
+                                  visibility_map=self.visibility_map)
         return self._tracer
 
     def Render(self, band: int, sound: int, absorbtion_factor: float, num_samples: int, dry: float,
