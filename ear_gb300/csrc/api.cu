@@ -296,21 +296,22 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   if (radius > 256) return fail(EAR_ERR_INVALID_ARG, "ploc_radius above 256");
   const int width = opts ? opts->width : 0;
   if (width != 0 && width != 2 && width != 4) return fail(EAR_ERR_INVALID_ARG, "width must be 0, 2 or 4");
-  cudaError_t e = build_lbvh(s->ds, pad, max_leaf, builder == EAR_BVH_PLOC ? kBuilderPloc : kBuilderLbvh,
-                             radius, 0, msg, sizeof msg);
-  s->ds.wide = width == 4 || (width == 0 && s->ds.num_tris >= kWideFrom);
   const int order = opts ? opts->visibility_order : 0;
   if (order < 0 || order > 2) return fail(EAR_ERR_INVALID_ARG, "visibility_order must be 0, 1 or 2");
-  s->ds.any_order = order;
-  s->ds.any_far = order == 2 ? 1 : 0;
-  s->probe_valid = false;
   const int vmap = opts ? opts->visibility_map : 0;
   if (vmap < -1 || (vmap > 0 && (vmap < 8 || vmap > 2048)))
     return fail(EAR_ERR_INVALID_ARG, "visibility_map must be -1, 0 or 8..2048");
-  s->vis_opt = vmap;
+  cudaError_t e = build_lbvh(s->ds, pad, max_leaf, builder == EAR_BVH_PLOC ? kBuilderPloc : kBuilderLbvh,
+                             radius, 0, msg, sizeof msg);
+  // the triangles' leaf order changed: the visibility maps address them
   free_vis_map(&s->vis);
   s->vis_valid = false;
   ++s->bvh_gen;
+  s->vis_opt = vmap;
+  s->ds.wide = width == 4 || (width == 0 && s->ds.num_tris >= kWideFrom);
+  s->ds.any_order = order;
+  s->ds.any_far = order == 2 ? 1 : 0;
+  s->probe_valid = false;
   if (e != cudaSuccess) {
     s->bvh = false;
     return fail(e == cudaErrorMemoryAllocation ? EAR_ERR_OUT_OF_MEMORY : EAR_ERR_CUDA,
