@@ -80,5 +80,8 @@ def test_map_walk_equals_the_brute_force_visibility_test(walker, seed):
     queries, blocked = int(fields["queries"]), int(fields["blocked"])
     assert queries > 100_000 and 0.2 * queries < blocked < 0.8 * queries
     assert int(fields["mismatches"]) == 0
+    print("reported hits: point at t", fields["worst_outside_over_pad"],
+          "x box_pad outside the box, exact crossing", fields["worst_crossing_over_pad"],
+          "x box_pad, crossing parameter", fields["worst_t_beyond"], "beyond [0, 1]")
     # the lists test a small part of the triangles the brute force tests
     assert int(fields["map_tests"]) * 10 < int(fields["brute_tests"])

@@ -11,8 +11,14 @@
 //                distance is within the walk's cut,
 // with the Moller-Trumbore test in both evaluation orders the trace kernels
 // use (exact kernels divide first; fast kernels compare unscaled).  The map
-// may only test fewer triangles, never decide differently.  Prints the
-// counts; exit status 1 on any mismatch.
+// may only test fewer triangles, never decide differently.  It also
+// reports, over every reported hit, how far outside the triangle's
+// unpadded box (in units of the tree's padding box_pad) lie the point at
+// the reported t and the exact crossing of the segment's line with the
+// triangle's plane (both in double), and how far that crossing's parameter
+// lies outside [0, 1]: the quantities the padding argument bounds.  For
+// segments grazing a triangle's plane the float test's rounding exceeds
+// them.  Prints the counts; exit status 1 on any mismatch.
 //
 // Built by tests/test_vismap_geom.py with nvcc, host code only, no
 // contraction (-ffp-contract=off).
@@ -96,6 +102,9 @@ int main(int argc, char** argv) {
   g_state ^= argc > 2 ? (uint64_t)atoll(argv[2]) * 0x9E3779B97F4A7C15ull : 0ull;
   const int resolutions[3] = {16, 128, 1024};
   long queries = 0, blocked = 0, mismatches = 0, tested_brute = 0, tested_map = 0;
+  double worst_outside = 0.0;  // largest (distance outside the box) / box_pad
+  double worst_crossing = 0.0;  // the same for the exact crossing point
+  double worst_t = -1.0;        // largest distance of its parameter outside [0, 1]
   std::vector<Tri> tris;
   for (int c = 0; c < cases; ++c) {
     const int res = resolutions[c % 3];
@@ -167,7 +176,32 @@ int main(int argc, char** argv) {
       for (const Tri& T : tris) {
         float t;
         ++tested_brute;
-        if (mt(T.v0, T.e1, T.e2, p, sdir, fast, t) && t > 1e-5f && t < 1.0f) hit_brute = true;
+        if (mt(T.v0, T.e1, T.e2, p, sdir, fast, t) && t > 1e-5f && t < 1.0f) {
+          hit_brute = true;
+          const double q[3] = {p.x + (double)t * sdir.x, p.y + (double)t * sdir.y,
+                               p.z + (double)t * sdir.z};
+          for (int k = 0; k < 3; ++k) {
+            const double lo = fmin(fmin(T.v[k], T.v[3 + k]), T.v[6 + k]);
+            const double hi = fmax(fmax(T.v[k], T.v[3 + k]), T.v[6 + k]);
+            const double out = fmax(fmax(lo - q[k], q[k] - hi), 0.0);
+            worst_outside = fmax(worst_outside, out / box_pad);
+          }
+          // exact crossing of the segment's line with the triangle's plane
+          const double e1[3] = {T.e1.x, T.e1.y, T.e1.z}, e2[3] = {T.e2.x, T.e2.y, T.e2.z};
+          const double nrm[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                 e1[0] * e2[1] - e1[1] * e2[0]};
+          const double d[3] = {sdir.x, sdir.y, sdir.z};
+          const double w[3] = {(double)T.v0.x - p.x, (double)T.v0.y - p.y, (double)T.v0.z - p.z};
+          const double nd = nrm[0] * d[0] + nrm[1] * d[1] + nrm[2] * d[2];
+          const double te = (nrm[0] * w[0] + nrm[1] * w[1] + nrm[2] * w[2]) / nd;
+          worst_t = fmax(worst_t, fmax(-te, te - 1.0));
+          for (int k = 0; k < 3; ++k) {
+            const double x = p.x * (k == 0) + p.y * (k == 1) + p.z * (k == 2) + te * d[k];
+            const double lo = fmin(fmin(T.v[k], T.v[3 + k]), T.v[6 + k]);
+            const double hi = fmax(fmax(T.v[k], T.v[3 + k]), T.v[6 + k]);
+            worst_crossing = fmax(worst_crossing, fmax(fmax(lo - x, x - hi), 0.0) / box_pad);
+          }
+        }
         if (listed(T, f, iu, iv, res) && T.dist <= cut) {
           ++tested_map;
           if (mt(T.v0, T.e1, T.e2, p, sdir, fast, t) && t > 1e-5f && t < 1.0f) hit_map = true;
@@ -182,7 +216,9 @@ int main(int argc, char** argv) {
       }
     }
   }
-  printf("cases %d queries %ld blocked %ld mismatches %ld brute_tests %ld map_tests %ld\n", cases,
-         queries, blocked, mismatches, tested_brute, tested_map);
+  printf("cases %d queries %ld blocked %ld mismatches %ld brute_tests %ld map_tests %ld "
+         "worst_outside_over_pad %.6f worst_crossing_over_pad %.6f worst_t_beyond %.3g\n",
+         cases, queries, blocked, mismatches, tested_brute, tested_map, worst_outside,
+         worst_crossing, worst_t);
   return mismatches ? 1 : 0;
 }
