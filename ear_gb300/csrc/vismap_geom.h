@@ -12,7 +12,10 @@
 // z).  The lists are conservative: the tree traversal already relies on
 // every point where the triangle test can report a hit lying inside the
 // triangle's box padded by box_pad, and the maps pad by P = 2 box_pad,
-// which also covers the rounding of the segment's direction.
+// which also covers the rounding of the segment's direction.  (For a
+// segment grazing a triangle's plane the test's rounding can report a
+// crossing farther out; neither the tree nor the maps are sure to
+// reproduce such an artefact.)
 #pragma once
 
 #include <math.h>
