@@ -76,7 +76,7 @@ bool derive_material(const ear_material& m, DevMaterial* o) {
 }
 
 int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job,
-                     std::vector<DevRecorder>* out) {
+                     DevRecorder* out) {
   int tracks = 0;
   for (int i = 0; i < nrec; ++i) {
     const ear_recorder& r = recs[i];
@@ -84,7 +84,7 @@ int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job
       fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
       return -1;
     }
-    DevRecorder d;
+    DevRecorder& d = out[i];
     for (int k = 0; k < 3; ++k) {
       d.loc[k] = r.location[k];
       d.right[k] = r.right_ear[k];
@@ -98,7 +98,6 @@ int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job
     d.job = job;
     d.vis_index = i;
     tracks += r.channels;
-    out->push_back(d);
   }
   return tracks;
 }
@@ -584,8 +583,8 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
     return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   if (src->num_emitter_triangles < 0 || (src->num_emitter_triangles > 0 && !src->emitter_vertices))
     return fail(EAR_ERR_INVALID_ARG, "bad emitter triangles");
-  std::vector<DevRecorder> dr;
-  const int tracks = derive_recorders(recs, nrec, 0, 0, &dr);
+  std::vector<DevRecorder> dr((size_t)nrec);
+  const int tracks = derive_recorders(recs, nrec, 0, 0, dr.data());
   if (tracks < 0) return EAR_ERR_INVALID_ARG;
   TraceArgs& a = out->a;
   std::memset(&a, 0, sizeof a);
@@ -1148,25 +1147,8 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   if (p->num_rays > (1ull << 47) || p->first_ray > (1ull << 47) - p->num_rays)
     return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   DevRecorder dr[kMaxRecorders];
-  int tracks = 0;
-  for (int i = 0; i < nrec; ++i) {
-    const ear_recorder& r = recs[i];
-    if (r.channels != 1 && r.channels != 2)
-      return fail(EAR_ERR_INVALID_ARG, "recorder %d: channels must be 1 or 2", i);
-    DevRecorder& d = dr[i];
-    for (int k = 0; k < 3; ++k) {
-      d.loc[k] = r.location[k];
-      d.right[k] = r.right_ear[k];
-      const float h = powf_portable(1.0f - r.head_absorption[k], 4.0f);
-      d.habs[k] = (0.0f < h) ? h : 0.0f;
-    }
-    d.head_size = r.head_size;
-    d.channels = r.channels;
-    d.track0 = tracks;
-    d.job = 0;
-    d.vis_index = i;
-    tracks += r.channels;
-  }
+  const int tracks = derive_recorders(recs, nrec, 0, 0, dr);
+  if (tracks < 0) return EAR_ERR_INVALID_ARG;
   CU(cudaSetDevice(s->device));
   unsigned char* scratch = nullptr;
   ear_status rc = noalloc_scratch(s->device, &scratch);
@@ -1221,6 +1203,13 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     if (vis_map_key(s, recs, nrec, res) == s->vis_key) set_vis_args(s, a);
   }
 
+  // launch limits are checked before any device work is queued, so a
+  // rejected call leaves the caller's histogram and the scratch untouched
+  const size_t smem = trace_smem_bytes(s->num_mats, tracks, kModeForward, ops->block);
+  if (smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
+  int per_sm = 0;
+  CU(ops->occupancy(kModeForward, ops->block, smem, &per_sm));
+  if (per_sm < 1) per_sm = 1;
   cudaStream_t st = (cudaStream_t)p->stream;
   const int rows = tracks * 3;
   // the shared scratch keeps the previous call's contents: clear it
@@ -1231,11 +1220,6 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     k_init_first_last<<<(rows + 127) / 128, 128, 0, st>>>(a.first_last, rows);
     CU(cudaGetLastError());
   }
-  const size_t smem = trace_smem_bytes(s->num_mats, tracks, kModeForward, ops->block);
-  if (smem > 200 * 1024) return fail(EAR_ERR_INVALID_ARG, "too many materials for one launch");
-  int per_sm = 0;
-  CU(ops->occupancy(kModeForward, ops->block, smem, &per_sm));
-  if (per_sm < 1) per_sm = 1;
   CU(cudaEventRecord(s->ev0, st));
   CU(ops->trace(a, a.num_items > 0 ? s->sm_count * per_sm : 1, ops->block, smem, kModeForward, st));
   CU(cudaEventRecord(s->ev1, st));

@@ -443,7 +443,9 @@ ear_status ear_batch_create(ear_scene* const* scenes, int32_t num_scenes, const 
     d.num_recs = J.num_recorders;
     d.inv_amount = 1.0f / ray_amount(J.num_rays);
     d.gain2 = J.gain * J.gain;
-    const int t = derive_recorders(J.recorders, J.num_recorders, tracks, j, &b->recs);
+    const size_t rbase = b->recs.size();
+    b->recs.resize(rbase + (size_t)std::max(0, J.num_recorders));
+    const int t = derive_recorders(J.recorders, J.num_recorders, tracks, j, b->recs.data() + rbase);
     if (t < 0) {
       delete b;
       return EAR_ERR_INVALID_ARG;

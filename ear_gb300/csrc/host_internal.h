@@ -32,11 +32,12 @@ ear_status fail(ear_status st, const char* fmt, ...);
 bool derive_material(const ear_material& m, DevMaterial* o);
 
 // MonoRecorder / StereoRecorder constructors (src/StereoRecorder.cpp:53-57):
-// appends one DevRecorder per recorder with tracks numbered from
-// track_base; `job` is stored in each.  Returns the number of tracks, or
-// -1 (with the error set) for an invalid recorder.
+// writes one DevRecorder per recorder into out[0 .. nrec-1] with tracks
+// numbered from track_base; `job` is stored in each.  Returns the number of
+// tracks, or -1 (with the error set) for an invalid recorder.  Writes into
+// the caller's array so that the no-allocation render shares it.
 int derive_recorders(const ear_recorder* recs, int nrec, int track_base, int job,
-                     std::vector<DevRecorder>* out);
+                     DevRecorder* out);
 
 template <typename T>
 cudaError_t grow(T** p, size_t* cap, size_t n) {

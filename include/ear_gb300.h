@@ -428,9 +428,17 @@ ear_status ear_batch_tune(ear_batch* batch, const ear_tune_opts* opts, ear_tune_
    - Limits: at most 32 recorders (64 tracks); point sources only (an area
      emitter needs per-call scratch: EAR_ERR_UNSUPPORTED).  Larger requests
      are rejected with EAR_ERR_INVALID_ARG and a message.
+   - The call returns only after the render has completed: it reads the
+     path counters and the error flag back and synchronises `stream`
+     before returning, whether or not first_sample / last_sample / stats
+     are requested.  A real-time caller should run it from a worker
+     thread, not from the audio callback itself.
    - The first call on a device resolves the array's device address
      (cudaGetSymbolAddress) with that device current; make that first call
-     before any stream capture.
+     before any stream capture.  The address is cached for the life of
+     the process: after cudaDeviceReset (or any other teardown of the
+     device's primary context) the cached address is stale, so do not call
+     this entry point again in that process.
    - The array is shared by every call on the device and keeps the last
      call's contents (each call clears what must start at zero).  Calls
      whose GPU work overlaps -- e.g. on two streams -- race on it: serialise

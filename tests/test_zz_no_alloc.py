@@ -42,10 +42,17 @@ def test_noalloc_matches_render_twice(exact):
         ref = tr.render(w.source, w.recorders, exact=exact, **kw)
         params = make_params(exact=exact, **kw)
         out = torch.empty((w.num_tracks, 3, kw["num_bins"]), dtype=torch.float32, device="cuda")
-        for _ in range(2):
+        for call in range(2):
             out.fill_(123.0)  # the call must zero the buffer itself
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             rc, first, last, stats = _noalloc(tr, w, params, out)
+            torch.cuda.synchronize()
             assert rc == N.EAR_OK, N.lib().ear_last_error()
+            if call:
+                # the defining property: once the first call has resolved
+                # the scratch address, a call takes no device memory
+                assert torch.cuda.mem_get_info()[0] == free0
             got = out.cpu().numpy()
             e_got, e_ref = _energy(got), _energy(ref.hist)
             assert (np.abs(e_got - e_ref) <= 1e-5 * np.maximum(e_ref, 1e-300)).all()
@@ -86,7 +93,7 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
     kw = dict(w.render)
     kw["num_rays"] = 10
     with Tracer(w.vertices, w.material_ids, w.materials, device=0) as tr:
-        out = torch.empty((2 * 33, 3, kw["num_bins"]), dtype=torch.float32, device="cuda")
+        out = torch.full((2 * 33, 3, kw["num_bins"]), 7.0, dtype=torch.float32, device="cuda")
         params = make_params(**kw)
         src, _ = w.source.at(-1)
         many = recorders_at(w.recorders * 17, -1)  # 34 recorders
@@ -103,3 +110,5 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
         rc = N.lib().ear_render_noalloc(tr._h, C.byref(src), recs, 2, C.byref(odd),
                                         out.data_ptr(), None, None, None)
         assert rc == N.EAR_ERR_INVALID_ARG and b"multiple of 4" in N.lib().ear_last_error()
+        # rejected calls queue no device work: the caller's buffer is as it was
+        assert bool((out == 7.0).all())
