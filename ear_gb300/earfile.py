@@ -102,9 +102,12 @@ def write_ear(path, **kw) -> None:
         f.write(encode(**kw))
 
 
-def workload_to_ear(w, samples: int, keys=None) -> bytes:
+def workload_to_ear(w, samples: int, keys=None, source_file: str = "dry.wav") -> bytes:
     """Encode a ``scenes.Workload`` (one MESH block per material, in
-    material order, so triangle order follows material_ids grouping)."""
+    material order, so triangle order follows material_ids grouping).
+    ``source_file`` names the source's WAV; the reference's source printout
+    wants a path with a directory (src/HelperFunctions.cpp:49-54), as the
+    Blender exporter writes them."""
     mats = []
     for m in w.materials:
         mats.append((m.name, m.reflection, m.refraction if m.refraction is not None else
@@ -117,7 +120,7 @@ def workload_to_ear(w, samples: int, keys=None) -> bytes:
     air = list(w.render.get("air_absorption", (0.0, 0.0, 0.0)))
     settings = {"debug": 0, "absorption": air, "drylevel": float(w.render.get("dry", 1.0)),
                 "samples": int(samples), "maxthreads": 8}
-    src = {"file": "dry.wav", "location": w.source.location, "gain": float(w.source.gain)}
+    src = {"file": source_file, "location": w.source.location, "gain": float(w.source.gain)}
     recs = []
     for r in w.recorders:
         recs.append({"file": "out.wav", "location": r.location, "channels": r.channels,

@@ -2,9 +2,12 @@
 
 TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
 the CPU-baseline legs of bench.py, as the checker or the timed baseline.
-The product (ear_gb300) never imports this package.  PARITY UNPINNED for
-the ray-tracing path (see the header of ear_oracle.cpp); the band split is
-pinned to the reference's own equalizer (oracle/_ref).
+The product (ear_gb300) never imports this package.  Pinned to the
+reference itself: the ray-tracing restatement equals, bit for bit, the
+reference's own Scene::Render compiled from its sources into oracle/_ref
+(tests/test_ref_pin.py; a committed fixture of its output,
+tests/golden/reference_render.json, pins it where the reference tree is
+absent), and the band split equals the reference's own equalizer.
 """
 from __future__ import annotations
 
@@ -254,3 +257,139 @@ def convolve_fft64(contexts, out_length):
         total += t
         caps.append(cap)
     return total, caps
+
+
+# ------------------------------------------------ the reference's own render
+# oracle/_ref/libear_ref_render.so (built by oracle/build_ref.py where the
+# reference tree exists): the reference's Scene::Render and parsers,
+# compiled against a GMTL / Boost interface shim whose random generator
+# replays a tape of uniforms recorded by the oracle.
+
+REF_RENDER_PATH = Path(__file__).resolve().parent / "_ref" / "libear_ref_render.so"
+_R = None
+
+
+def ref_render_lib():
+    """The reference-built render library, or None where it was not built."""
+    global _R
+    if _R is None:
+        if not REF_RENDER_PATH.exists():
+            return None
+        lib()  # the oracle library it links (portable power function)
+        R = C.CDLL(str(REF_RENDER_PATH))
+        R.ref_render_band.restype = C.c_int
+        R.ref_render_band.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
+                                      C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]
+        R.ref_last_error.restype = C.c_char_p
+        lib().oracle_random_tape.restype = C.c_int
+        lib().oracle_random_tape.argtypes = [C.POINTER(N.EarSceneDesc), C.POINTER(N.EarSource),
+                                             C.POINTER(N.EarRecorder), C.c_int32,
+                                             C.POINTER(N.EarRenderParams), C.c_void_p, C.c_int64,
+                                             C.c_void_p]
+        _R = R
+    return _R
+
+
+def random_tape(vertices, material_ids, materials, source, recorders, *, band, keyframe=-1,
+                **kw):
+    """The uniforms a single-threaded oracle render of one band consumes, in
+    the order the reference's global generator is called for the same
+    paths (float32 array)."""
+    ref_render_lib()
+    d, keep = scene_desc(vertices, material_ids, materials)
+    src, _k2 = source.at(keyframe)
+    recs = recorders_at(recorders, keyframe)
+    p = make_params(**dict(kw, bands=(band,)))
+    used = C.c_int64(0)
+    rc = lib().oracle_random_tape(C.byref(d), C.byref(src), recs, len(recorders), C.byref(p),
+                                  None, 0, C.byref(used))
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+    tape = np.empty(max(1, used.value), np.float32)
+    rc = lib().oracle_random_tape(C.byref(d), C.byref(src), recs, len(recorders), C.byref(p),
+                                  tape.ctypes.data, tape.size, C.byref(used))
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+    return tape[:used.value]
+
+
+def reference_render_band(ear_path, band, num_rays, tape, window, max_tracks=64):
+    """Runs the reference's Scene::Render for one band on a .EAR file with
+    `tape` as its random numbers.  Returns (tracks[:, :window], first_sample,
+    real_length, uniforms consumed)."""
+    R = ref_render_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libear_ref_render.so is not built")
+    t = np.ascontiguousarray(tape, np.float32)
+    out = np.zeros((max_tracks, window), np.float32)
+    first = np.zeros(max_tracks, np.int32)
+    real = np.zeros(max_tracks, np.int32)
+    used = C.c_int64(0)
+    n = R.ref_render_band(str(ear_path).encode(), int(band), int(num_rays), t.ctypes.data, t.size,
+                          C.byref(used), int(window), int(max_tracks), out.ctypes.data,
+                          first.ctypes.data, real.ctypes.data)
+    if n < 0:
+        raise RuntimeError("reference render: " + R.ref_last_error().decode())
+    return out[:n], first[:n], real[:n], used.value
+
+
+def grouped_by_material(w):
+    """(vertices, material_ids) of a workload in the order a .EAR file
+    lists them (one MESH block per material, in material order) -- the
+    triangle order of the reference's combined mesh (src/Scene.cpp:103-106)."""
+    order = np.argsort(w.material_ids, kind="stable")
+    return w.vertices[order], w.material_ids[order]
+
+
+def write_reference_scene(w, directory) -> Path:
+    """Writes `w` as scene.ear (with a short silent dry.wav beside it, named
+    by its full path as the Blender exporter writes it) into `directory`."""
+    import wave
+
+    from ear_gb300 import earfile
+
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    wav = d / "dry.wav"
+    with wave.open(str(wav), "wb") as f:
+        f.setnchannels(1)
+        f.setsampwidth(2)
+        f.setframerate(44100)
+        f.writeframes(np.zeros(64, np.int16).tobytes())
+    ear = d / "scene.ear"
+    ear.write_bytes(earfile.workload_to_ear(w, samples=1000, source_file=str(wav.resolve())))
+    return ear
+
+
+def reference_pin_params(w, num_rays, window):
+    """Render arguments under which the oracle follows the reference's own
+    loop: at most 1000 path vertices and the fixed 1e-8 cut-off
+    (src/Scene.cpp:142,275)."""
+    kw = dict(w.render)
+    kw.update(num_rays=int(num_rays), max_bounces=N.EAR_REFERENCE_MAX_BOUNCES,
+              cutoff=N.EAR_REFERENCE_CUTOFF, num_bins=int(window))
+    return kw
+
+
+def reference_render(w, directory, num_rays, window, bands=(0, 1, 2)):
+    """The reference's own Scene::Render of workload `w` (point source,
+    static) per band, on the oracle's random tape for the same rays.
+    Returns dict(tracks (tracks, 3, window) float32, first_sample /
+    real_length (tracks, 3), tape and used (per band))."""
+    V, M = grouped_by_material(w)
+    ear = write_reference_scene(w, directory)
+    kw = reference_pin_params(w, num_rays, window)
+    ntr = sum(r.tracks for r in w.recorders)
+    out = {"tracks": np.zeros((ntr, 3, window), np.float32),
+           "first_sample": np.zeros((ntr, 3), np.int64), "real_length": np.zeros((ntr, 3), np.int64),
+           "tape": [0, 0, 0], "used": [0, 0, 0]}
+    for b in bands:
+        tape = random_tape(V, M, w.materials, w.source, w.recorders, band=b, **kw)
+        tr, first, real, used = reference_render_band(ear, b, num_rays, tape, window)
+        out["tracks"][:, b] = tr
+        out["first_sample"][:, b] = first
+        out["real_length"][:, b] = real
+        out["tape"][b] = len(tape)
+        out["used"][b] = used
+    return out

@@ -5,18 +5,25 @@
 // and only as the checker or the timed CPU baseline; the product path never
 // calls it.
 //
-// PARITY UNPINNED against the reference binary: the reference cannot be
-// compiled here (it needs GMTL 0.6.1 and Boost.Thread, neither vendored nor
-// installed) and it ships no tests, golden vectors or .EAR fixtures.  This
-// file restates the reference's algorithm step by step from its sources
-// (citations are path:line inside aothms/ear) with three documented
-// substitutions that both this oracle and the CUDA path share by
-// specification:
+// PINNED to the reference itself.  The reference's shipped build cannot
+// run here (GMTL 0.6.1 and Boost.Thread are neither vendored nor
+// installed, and it ships no tests, golden vectors or .EAR fixtures), so
+// oracle/build_ref.py compiles its own ray-tracing sources (src/Scene,
+// Mesh, Triangle, Material, Mono/StereoRecorder, Recorder, Datatype, ...)
+// against a project-written GMTL / Boost interface shim (oracle/refshim/)
+// into oracle/_ref, and tests/test_ref_pin.py checks that its
+// Scene::Render, fed this oracle's random numbers in its own call order
+// (oracle_random_tape), writes FloatBuffer tracks bit-identical to this
+// file's float accumulation.  This file restates the reference's algorithm
+// step by step from its sources (citations are path:line inside
+// aothms/ear) with three documented substitutions that this oracle, the
+// CUDA path and the shim share by specification:
 //   1. gmtl::Math::unitRandom (a global, time-seeded PRNG) is replaced by a
 //      counter-based Philox-4x32-10 stream (Salmon et al., SC'11) indexed by
 //      (seed, context, band, ray, bounce, try), so every draw is addressable.
 //   2. gmtl::intersectDoubleSided is restated from Moller & Trumbore (1997),
-//      non-culling variant, epsilon 1e-6, in a fixed operation order.
+//      non-culling variant, epsilon 1e-6, in a fixed operation order.  GMTL
+//      is not vendored, so this one function is not pinned to it.
 //   3. pow() is the project-defined portable_powf() below (exp2(y*log2 x)
 //      with an atanh series for the log and a Taylor polynomial for exp2),
 //      so the cut-off decision at src/Scene.cpp:275 cannot diverge between
@@ -184,6 +191,14 @@ struct Rng {
 
 constexpr int kMaxTries = 256;
 
+// Random tape (oracle_random_tape): when set, every uniform a trace
+// consumes is appended in the order the reference's single global
+// generator would be called for the same path -- per reflection the
+// material choice (src/Material.cpp:82) before the direction tries
+// (src/Scene.cpp:59-71), each try's three draws in Sample_Sphere's order
+// (src/Distributions.h:49-51).  Single-threaded renders only.
+thread_local std::vector<float>* g_tape = nullptr;
+
 // Sample_Sphere (src/Distributions.h:48-58) and Sample_Hemi
 // (src/Distributions.h:62-67): rejection in the cube, reject l<0.001 or
 // l>1, then (hemisphere) reject dot(n,v) < 0.  One Philox block per try.
@@ -192,6 +207,8 @@ constexpr int kMaxTries = 256;
 bool sample_dir(const Rng& rng, uint64_t ray, uint32_t bounce, const V3* n, V3* out) {
   for (int tr = 0; tr < kMaxTries; ++tr) {
     const U4 b = rng.block(ray, 0, bounce, (uint32_t)tr);
+    if (g_tape)
+      for (int q = 0; q < 3; ++q) g_tape->push_back(uniform24(b.v[q]));
     const float f1 = uniform24(b.v[0]) * 2.0f - 1.0f;
     const float f2 = uniform24(b.v[1]) * 2.0f - 1.0f;
     const float f3 = uniform24(b.v[2]) * 2.0f - 1.0f;
@@ -469,10 +486,15 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
         // (src/Triangle.cpp:44-53)
         const U4 b = rng.block(ray, 1, 0, 0);
         float x = uniform24(b.v[0]) * em->total_area;
+        if (g_tape) g_tape->push_back(uniform24(b.v[0]));
         V3 p = {0, 0, 0}, en = {0, 0, 0};
         for (size_t i = 0; i < em->area.size(); ++i) {
           x -= em->area[i];
           if (x < 0) {
+            if (g_tape) {
+              g_tape->push_back(uniform24(b.v[1]));
+              g_tape->push_back(uniform24(b.v[2]));
+            }
             const float r1 = uniform24(b.v[1]);
             const float r2 = uniform24(b.v[2]);
             const float sr1 = std::sqrt(r1);
@@ -505,6 +527,7 @@ void trace_ray(const OScene& sc, const Emitter* em, V3 src, const std::vector<OR
       // Material::Bounce (src/Material.cpp:76-83)
       if (!M.always_reflect[band]) {
         const U4 b = rng.block(ray, 0, (uint32_t)k, 0);
+        if (g_tape) g_tape->push_back(uniform24(b.v[3]));
         bt = (uniform24(b.v[3]) <= M.p_reflect[band]) ? 0 : 1;
       }
       if (adj) {
@@ -885,6 +908,36 @@ int oracle_render(const ear_scene_desc* desc, const ear_source* source,
                   oracle_output* out) {
   return render_impl(desc, source, recorders, num_recorders, params, num_threads, pow_mode, out,
                      nullptr, nullptr);
+}
+
+// The uniforms a single-threaded render of one band consumes, in the order
+// the reference's global generator is called (see g_tape): up to `cap`
+// values into `tape`, the full count in *used.  Same arguments as
+// oracle_render; bands_mask must select exactly one band.
+int oracle_random_tape(const ear_scene_desc* desc, const ear_source* source,
+                       const ear_recorder* recorders, int32_t num_recorders,
+                       const ear_render_params* params, float* tape, int64_t cap,
+                       int64_t* used) {
+  if (!params || (params->bands_mask != 1u && params->bands_mask != 2u && params->bands_mask != 4u) ||
+      !used || (cap > 0 && !tape)) {
+    std::snprintf(g_err, sizeof g_err, "invalid argument");
+    return 1;
+  }
+  std::vector<float> t;
+  g_tape = &t;
+  const int nb = params->num_bins > 0 ? params->num_bins : 1;
+  int ntr = 0;
+  for (int i = 0; i < num_recorders; ++i) ntr += recorders[i].channels == 2 ? 2 : 1;
+  std::vector<double> h64((size_t)std::max(1, ntr) * 3 * (size_t)nb);
+  oracle_output out;
+  std::memset(&out, 0, sizeof out);
+  out.hist64 = h64.data();
+  const int rc = render_impl(desc, source, recorders, num_recorders, params, 1, 0, &out, nullptr,
+                             nullptr);
+  g_tape = nullptr;
+  *used = (int64_t)t.size();
+  if (cap > 0) std::memcpy(tape, t.data(), sizeof(float) * (size_t)std::min<int64_t>(cap, *used));
+  return rc;
 }
 
 // FP64 reference gradient of L = sum(g * h) with respect to each material's

@@ -1,6 +1,9 @@
 """Generates the golden fixtures in this directory.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference REFERENCE_ROOT]
+
+REFERENCE_ROOT defaults to $EAR_REFERENCE_ROOT, else to a checkout named
+``reference`` beside this repository.
 
 * material_presets.json -- the 7 material presets of the reference's Blender
   add-on, read by importing blender/render_EAR/materials.py from the
@@ -102,7 +105,8 @@ def oracle_shoebox():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    default = os.environ.get("EAR_REFERENCE_ROOT") or os.path.join(HERE, "..", "..", "..", "reference")
+    ap.add_argument("--reference", default=os.path.normpath(default))
     args = ap.parse_args()
     pre = presets(args.reference)
     with open(os.path.join(HERE, "material_presets.json"), "w") as f:

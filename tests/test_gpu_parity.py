@@ -241,3 +241,32 @@ def test_sah_cost_ranks_the_builders():
     for b2, b4 in costs.values():
         assert np.isfinite(b2) and np.isfinite(b4) and b2 > 1.0 and b4 > 1.0
     assert costs["ploc"][0] < costs["lbvh"][0]
+
+
+def test_exact_render_matches_the_reference_fixture():
+    """The exact kernels against the reference's own Scene::Render output
+    (tests/golden/reference_render.json, made from the reference's sources
+    compiled on the CPU; the oracle reproduces it bit for bit,
+    tests/test_ref_pin.py): identical first_sample / real_length
+    bookkeeping, per-band energies and 64 time-block energies within 1e-5
+    (only the order of the float additions differs)."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).resolve().parent / "golden" / "reference_render.json").read_text())
+    makers = {"small_test_room": scenes.small_test_room, "shoebox": scenes.shoebox}
+    for case in g["cases"]:
+        w = makers[case["name"]]()
+        V, M = oracle.grouped_by_material(w)
+        kw = oracle.reference_pin_params(w, case["rays"], case["window"])
+        with Tracer(V, M, w.materials, device=0) as tr:
+            res = tr.render(w.source, w.recorders, exact=True, **kw)
+        for t, row in enumerate(case["tracks"]):
+            for b, ref in enumerate(row):
+                assert int(res.first_sample[t, b]) == ref["first_sample"], (case["name"], t, b)
+                assert int(res.last_sample[t, b]) == min(ref["real_length"], case["window"])
+                e = res.hist[t, b].astype(np.float64) ** 2
+                assert abs(e.sum() - ref["energy"]) <= 1e-5 * ref["energy"], (case["name"], t, b)
+                blocks = np.array([c.sum() for c in np.array_split(e, 64)])
+                refb = np.array(ref["block_energy"])
+                assert (np.abs(blocks - refb) <= 1e-5 * ref["energy"]).all(), (case["name"], t, b)
