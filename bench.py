@@ -4,8 +4,10 @@
 A step is one ear_render of the workload: every band of the (source,
 keyframe) context, all rays, all recorders -- one pass of the hot path
 (Scene::Render, src/Scene.cpp:111-318) over its synthetic scene.  The
-default workload is the 20,000-triangle relief hall (stereo recorder, 3 s
-histograms, 200 reflections) at 1e7 rays per band.
+default workload is the 2,000,000-triangle cathedral (1 stereo + 8 mono
+recorders, 12 materials, 4 s histograms, 300 reflections) at 1e8 rays per
+band; the 20,000-triangle relief hall (1e7 rays per band) is reported
+beside it in `relief_hall`.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
   python bench.py --impl reference ...   # the reference algorithm on the CPU
@@ -14,12 +16,19 @@ value      segments/s over the K timed steps, scene resident in HBM, device
            time (CUDA events around each step on its stream; the L2 is
            flushed with a 512 MB write before every step, outside the step).
 e2e        the same metric through the C ABI from host memory: scene upload
-           from pinned host buffers, LBVH build, render, histograms read back
-           to the host, scene release -- all inside each timed step.
+           from pinned host buffers, BVH and visibility-map builds, render,
+           histograms read back to the host, scene release -- all inside
+           each timed step.
 roofline   algorithmic bytes of the trace kernel (64 B per node visit, 48 B
-           per triangle test, 64 B of path state per segment, 4 B per splat
-           bin; counted on the device) / its CUDA-event time, against the
-           measured HBM copy bandwidth.
+           per triangle test, 8 B per visibility-map entry, 64 B of path
+           state per segment, 4 B per splat bin; counted on the device) /
+           its CUDA-event time, against the measured HBM copy bandwidth;
+           `l2_frac` against an L2-resident copy measured in the same run.
+accuracy   the benchmarked fast kernels against the exact kernels (bit-exact
+           to the oracle) on the same rays: largest per-band EDC difference
+           down to -40 dB and largest relative T60 difference.
+adjoint_ratio  ear_render_adjoint time / ear_render time (configs' inverse
+           shoebox, 1e6 rays per band).
 cpu_baseline  the CPU restatement of the reference algorithm (brute-force
            triangle loops, oracle/), all host threads, on a bounded ray sample.
 auralisation  the steps after the impulse responses (band split, FFT and
@@ -175,18 +184,29 @@ def sum_over_ranks(x: float, world: int) -> float:
 
 
 def cpu_baseline(w, sample_rays: int, threads: int):
-    """The CPU restatement of the reference path on a bounded ray sample."""
+    """The CPU restatement of the reference path on a bounded ray sample:
+    the three bands run at once (as the reference's per-band contexts do),
+    each band's rays split over threads // 3 threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
     import oracle
 
     kw = dict(w.render)
     kw["num_rays"] = sample_rays
+    per_band = max(1, threads // 3)
+
+    def band(b):
+        return oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
+                             threads=per_band, **dict(kw, bands=(b,)))
+
     t0 = time.perf_counter()
-    r = oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
-                      threads=threads, **kw)
+    with ThreadPoolExecutor(max_workers=3) as ex:  # ctypes releases the GIL
+        rs = list(ex.map(band, range(3)))
     dt = time.perf_counter() - t0
-    seg = r["counters"]["segments"]
-    return {"value": seg / dt, "unit": "segments/s", "cores": threads, "kind": "port",
-            "sample": f"{sample_rays} rays/band x 3 bands of the same workload "
+    seg = sum(r["counters"]["segments"] for r in rs)
+    cores = min(threads, 3 * per_band)
+    return {"value": seg / dt, "unit": "segments/s", "cores": cores, "kind": "port",
+            "sample": f"{sample_rays} rays/band x 3 bands of the same workload, bands at once "
                       f"({seg} segments, {dt:.1f} s, brute-force triangle loops)",
             "seconds": dt, "segments": seg}
 
@@ -212,8 +232,10 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": _config(w, args, flush="n/a (CPU)"),
-        "cpu_baseline": {"value": v, "unit": "segments/s", "cores": threads, "kind": "port",
+        "config": _config(w, args),
+        "run": {"l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "segments/s", "cores": 3 * max(1, threads // 3),
+                         "kind": "port",
                          "sample": f"{sample} rays/band x 3 bands per step of the workload, "
                                    "brute-force O(T) loops as the reference"},
         "e2e": {"value": v, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -223,16 +245,17 @@ def run_reference(args):
 
 
 def _default_cpu_rays(name):
-    return {"relief_hall": 4000, "shoebox": 20000, "cathedral": 4}.get(name, 100)
+    return {"relief_hall": 4000, "shoebox": 20000, "cathedral": 5}.get(name, 100)
 
 
-def _config(w, args, flush):
+def _config(w, args):
+    """The workload, identical in both arms' lines; how each arm ran it
+    goes beside it (`run`)."""
     return {"workload": w.name, "triangles": w.num_triangles, "materials": len(w.materials),
             "recorders": len(w.recorders), "tracks": w.num_tracks,
             "rays_per_band": w.render["num_rays"], "bands": 3,
             "max_bounces": w.render["max_bounces"], "histogram_bins": w.render["num_bins"],
-            "cutoff": w.render["cutoff"], "parallelism": f"replicas{args.gpus}",
-            "l2": flush}
+            "cutoff": w.render["cutoff"], "parallelism": f"replicas{args.gpus}"}
 
 
 def adjoint_ratio(device: int, rays: int, steps: int):
@@ -286,14 +309,17 @@ def adjoint_ratio(device: int, rays: int, steps: int):
             "path": "ear_render (exact) vs ear_render_adjoint (exact, d_hist on device)"}
 
 
-def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_cache=None):
+def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_cache=None,
+                  curve: str = ""):
     """The batched sweep (16 convex rooms of 500..200,000 triangles, 16
     source / listener pairs each, sources on 24-keyframe paths, 2 s mono
     histograms, 3 bands) rendered two ways on the same GPU: the plain
     per-pair loop (one ear_render per pair-frame, histograms to the device)
     and one autotuned batched launch (ear_batch_run, graph replay).  Point
     1: every pair-frame at ``rays`` rays per band.  Point 2: one pair-frame
-    per room at ``full_rays`` rays (the configuration's ray count)."""
+    per room at ``full_rays`` rays (the configuration's ray count).  The
+    crossover `curve`: the 256 source/listener pairs at keyframe 0, at each
+    listed ray count, plus point 2."""
     import torch
 
     from ear_gb300 import Tracer, scenes
@@ -371,6 +397,21 @@ def batched_sweep(device: int, rays: int, keyframes: int, full_rays: int, tune_c
             "batched_ms": bms, "speedup": pms / bms,
             "plain_segments_per_s": pseg / (pms / 1000.0),
             "batched_segments_per_s": bseg / (bms / 1000.0), "segments_equal": pseg == bseg}
+    pts = [int(x) for x in curve.split(",") if x.strip()] if curve else []
+    if pts:
+        res["curve"] = []
+        for nr in pts:
+            jobs = jobs_for(nr, [0])
+            bms, bseg, cfg, _ = batched(jobs, False)
+            pms, pseg = plain(jobs)
+            res["curve"].append({"pair_frames": len(jobs), "rays_per_pair_frame": nr,
+                                 "plain_ms": pms, "batched_ms": bms, "speedup": pms / bms,
+                                 "segments_equal": pseg == bseg})
+        if "config_rays" in res:
+            c = res["config_rays"]
+            res["curve"].append({k: c[k] for k in ("pair_frames", "rays_per_pair_frame",
+                                                   "plain_ms", "batched_ms", "speedup",
+                                                   "segments_equal")})
     for t in tracers:
         t.close()
     return res
@@ -520,13 +561,118 @@ def auralisation(device: int, steps: int, cpu: bool):
     return res
 
 
-def run_ours(args):
-    import ctypes as C
+# DRAM traffic of the trace kernel per launch (dram__bytes_read.sum +
+# dram__bytes_write.sum) from ncu captures of the fast kernels with the
+# automatic visibility maps, keyed by (workload, rays per band); other
+# settings report null.  The cathedral figure is a capture at 1e6 rays per
+# band scaled to the 1e8-ray launch by the segments rendered (the traffic
+# of a persistent launch grows with the paths it traces).
+TRAFFIC_PER_LAUNCH = {
+    ("relief-hall-20k-stereo", 10_000_000): 219_903_488,
+}
 
+
+def l2_copy_gbs(dev, mbytes: int = 32, reps: int = 20) -> float:
+    """Bandwidth of a device-to-device copy whose source and destination
+    (2 x mbytes) stay resident in the 126 MB L2: read + write bytes over the
+    best CUDA-event time of `reps` copies."""
     import torch
 
-    from ear_gb300 import Tracer, _native as N
-    from ear_gb300.scene import make_params, recorders_at
+    n = mbytes * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(5):
+        b.copy_(a)
+    best = float("inf")
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.copy_(a)
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n * 4 / (best / 1000.0) / 1e9
+
+
+def alg_bytes(agg) -> float:
+    """Algorithmic bytes of the trace kernel: 64 B per node visit, 48 B per
+    triangle test, 64 B of path state per segment, 4 B per splat bin, 8 B
+    per visibility-map entry."""
+    return 64.0 * agg["node_visits"] + 48.0 * agg["triangle_tests"] + 64.0 * agg["segments"] \
+        + 4.0 * agg["splat_bins"] + 8.0 * agg["map_entries"]
+
+
+AGG_KEYS = ("node_visits", "triangle_tests", "splat_bins", "segments", "rays", "shadow_queries",
+            "map_entries")
+
+
+def timed_renders(tracer, w, kw, out, flush, stream, steps, warmup, exact, world):
+    """W warm-up and K timed renders of one workload; CUDA events around
+    each step on its stream, L2 flushed before each step (outside it)."""
+    import torch
+
+    def step():
+        return tracer.render(w.source, w.recorders, out=out, exact=exact, **kw)
+
+    map_build_ms = 0.0
+    for _ in range(max(3, warmup)):
+        map_build_ms += float(step().stats["map_build_ms"])
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    total_ms = kern_ms = 0.0
+    agg = {k: 0 for k in AGG_KEYS}
+    res = None
+    for _ in range(steps):
+        flush.fill_(1.0)
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        res = step()
+        s1.record(stream)
+        s1.synchronize()
+        total_ms += s0.elapsed_time(s1)
+        kern_ms += res.stats["kernel_ms"]
+        for k in agg:
+            agg[k] += int(res.stats[k])
+    torch.cuda.synchronize()
+    barrier(world)
+    return {"total_ms": total_ms, "kernel_ms": kern_ms, "agg": agg, "last": res,
+            "map_build_ms": map_build_ms}
+
+
+def roofline_of(t, steps, hbm, src, l2, traffic):
+    ab = alg_bytes(t["agg"])
+    ach = ab / (t["kernel_ms"] / 1000.0) / 1e9 if t["kernel_ms"] > 0 else 0.0
+    return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": traffic, "peak_source": src, "kernel": "fast::trace_kernel<0>",
+            "algorithmic_bytes_per_launch": ab / steps,
+            "kernel_ms_per_launch": t["kernel_ms"] / steps,
+            "l2_peak": l2, "l2_frac": ach / l2 if l2 else None,
+            "l2_peak_source": "device-to-device copy of 32 MB, L2-resident, measured in this run"}
+
+
+def accuracy(local, w, rays):
+    """The benchmarked fast kernels against the exact kernels (bit-exact to
+    the oracle) on the same rays: post.fast_exact_accuracy."""
+    from ear_gb300 import Tracer, post
+
+    kw = dict(w.render, num_rays=int(rays))
+    with Tracer(w.vertices, w.material_ids, w.materials, device=local) as tr:
+        fast = tr.render(w.source, w.recorders, exact=False, **kw)
+        exact = tr.render(w.source, w.recorders, exact=True, **kw)
+    acc = post.fast_exact_accuracy(fast, exact)
+    acc["rays_per_band"] = int(rays)
+    acc["within_target"] = bool(acc["edc_max_db"] < 0.5 and acc["t60_rel"] < 0.02)
+    return acc
+
+
+def run_ours(args):
+    import torch
+
+    from ear_gb300 import Tracer
 
     rank, world, local = dist_init(args.gpus)
     torch.cuda.set_device(local)
@@ -548,61 +694,26 @@ def run_ours(args):
     out = torch.zeros((tracks, 3, kw["num_bins"]), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    hbm, src = peaks()
 
-    def step():
-        return tracer.render(w.source, w.recorders, out=out, exact=exact, **kw)
-
-    map_build_ms = 0.0
-    for _ in range(max(3, args.warmup)):
-        map_build_ms += float(step().stats["map_build_ms"])
-    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
-    barrier(world)
-    torch.cuda.synchronize()
-    total_ms = 0.0
-    kern_ms = 0.0
-    seg = 0
-    agg = {"node_visits": 0, "triangle_tests": 0, "splat_bins": 0, "segments": 0, "rays": 0,
-           "shadow_queries": 0, "map_entries": 0}
-    launches = 0
     t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        s0 = torch.cuda.Event(enable_timing=True)
-        s1 = torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        res = step()
-        s1.record(stream)
-        s1.synchronize()
-        total_ms += s0.elapsed_time(s1)
-        kern_ms += res.stats["kernel_ms"]
-        for k in agg:
-            agg[k] += int(res.stats[k])
-        # per step: first/last init, the persistent trace kernel, finalize
-        launches += 3
-    torch.cuda.synchronize()
-    barrier(world)
+    t = timed_renders(tracer, w, kw, out, flush, stream, args.steps, args.warmup, exact, world)
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
-    t_max = max_over_ranks(total_ms, world)
+    t_max = max_over_ranks(t["total_ms"], world)
+    agg = t["agg"]
     seg_all = sum_over_ranks(agg["segments"], world)
     value = seg_all / (t_max / 1000.0)
-
-    # roofline of the trace kernel: algorithmic bytes / kernel time
-    alg_bytes = 64.0 * agg["node_visits"] + 48.0 * agg["triangle_tests"] + 64.0 * agg["segments"] \
-        + 4.0 * agg["splat_bins"] + 8.0 * agg["map_entries"]
-    achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else 0.0
-    hbm, src = peaks()
-    per_launch = alg_bytes / args.steps
-    # DRAM traffic of the trace kernel per launch, dram__bytes_read.sum +
-    # dram__bytes_write.sum from one ncu capture of this default workload
-    # (1e7 rays/band, fast kernels, automatic visibility map); other
-    # workloads and settings report null
+    # per step: first/last init, the persistent trace kernel, finalize
+    launches = 3 * args.steps
+    res = t["last"]
+    l2 = l2_copy_gbs(dev)
     traffic = None
-    if (w.name == "relief-hall-20k-stereo" and int(kw["num_rays"]) == 10_000_000 and not exact
-            and args.vismap == 0):
-        traffic = 219_903_488
+    if not exact and args.vismap == 0:
+        traffic = TRAFFIC_PER_LAUNCH.get((w.name, int(kw["num_rays"])))
+    roof = roofline_of(t, args.steps, hbm, src, l2, traffic)
 
     # e2e through the C ABI from pinned host memory, every step
     e2e = None
@@ -610,7 +721,7 @@ def run_ours(args):
         vp = torch.from_numpy(np.ascontiguousarray(w.vertices)).pin_memory().numpy()
         mp = torch.from_numpy(np.ascontiguousarray(w.material_ids)).pin_memory().numpy()
         host_out = torch.empty((tracks, 3, kw["num_bins"]), dtype=torch.float32).pin_memory()
-        e_steps = max(1, min(args.steps, 3))
+        e_steps = max(1, min(args.steps, args.e2e_steps))
         torch.cuda.synchronize()
         barrier(world)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -632,11 +743,40 @@ def run_ours(args):
                "d2h_bytes_per_step": int(host_out.numel() * 4),
                "steps": e_steps, "ms_per_step": e_ms / e_steps,
                "path": "ear_scene_create (pinned host) + ear_scene_build_bvh + ear_render "
-                       "(histograms to pinned host) + ear_scene_destroy"}
+                       "(histograms to pinned host; visibility maps built inside) + "
+                       "ear_scene_destroy"}
+
+    # the relief hall (configs' 20,000-triangle scene) beside the headline
+    relief = None
+    if not args.no_relief and args.workload != "relief_hall":
+        wr = load_workload("relief_hall", None)
+        kr = dict(wr.render, first_ray=rank * int(wr.render["num_rays"]))
+        with Tracer(wr.vertices, wr.material_ids, wr.materials, device=local) as trr:
+            outr = torch.zeros((wr.num_tracks, 3, kr["num_bins"]), dtype=torch.float32, device=dev)
+            rs = max(1, min(args.steps, 5))
+            tr_ = timed_renders(trr, wr, kr, outr, flush, stream, rs, 3, False, world)
+        rmax = max_over_ranks(tr_["total_ms"], world)
+        relief = {"config": _config(wr, args), "steps": rs,
+                  "value": sum_over_ranks(tr_["agg"]["segments"], world) / (rmax / 1000.0),
+                  "unit": "segments/s", "ms_per_step": rmax / rs,
+                  "rays_per_s": tr_["agg"]["rays"] / (tr_["total_ms"] / 1000.0) * world,
+                  "roofline": roofline_of(tr_, rs, hbm, src, l2,
+                                          TRAFFIC_PER_LAUNCH.get((wr.name, int(kr["num_rays"])))),
+                  "entries_read_per_segment":
+                      tr_["agg"]["map_entries"] / max(1, tr_["agg"]["segments"])}
+        launches += 3 * rs
+
+    acc = None
+    if not args.no_accuracy:
+        acc = {w.name: accuracy(local, w, args.accuracy_rays)}
+        if args.workload != "relief_hall":
+            acc["relief-hall-20k-stereo"] = accuracy(local, load_workload("relief_hall", None),
+                                                     args.accuracy_rays)
 
     bat = None
     if not args.no_batch:
-        bat = batched_sweep(local, args.batch_rays, args.batch_keyframes, args.batch_full_rays)
+        bat = batched_sweep(local, args.batch_rays, args.batch_keyframes, args.batch_full_rays,
+                            curve=args.batch_curve)
 
     adj = None
     if not args.no_adjoint:
@@ -654,44 +794,44 @@ def run_ours(args):
         cpu.pop("segments", None)
         # the reference's own threading: one thread per (source, keyframe,
         # band) context (src/EAR.cpp:193-207), i.e. 3 for one context
-        ref3 = cpu_baseline(w, max(1, sample // 4), 3)
+        ref3 = cpu_baseline(w, max(1, sample // 2), 3)
         cpu["reference_threading"] = {"value": ref3["value"], "unit": "segments/s",
-                                      "threads": 3, "sample_rays_per_band": max(1, sample // 4)}
+                                      "threads": 3, "sample_rays_per_band": max(1, sample // 2)}
 
     if rank == 0:
-        cfg = _config(w, args, flush="flushed before every step (512 MB write)")
-        cfg["mode"] = "exact (--fmad=false)" if exact else "fast"
-        cfg["bvh"] = tracer.info()
+        run = {"l2": "flushed before every step (512 MB write)",
+               "mode": "exact (--fmad=false)" if exact else "fast",
+               "bvh": tracer.info(),
+               "rays_per_s": agg["rays"] / (t["total_ms"] / 1000.0) * world}
         # tree quality beside segments/s (unit node and triangle costs)
-        cfg["bvh"]["sah_cost"] = {"binary": tracer.sah_cost(2), "wide4": tracer.sah_cost(4)}
+        run["bvh"]["sah_cost"] = {"binary": tracer.sah_cost(2), "wide4": tracer.sah_cost(4)}
         # listener visibility maps (built during warm-up, reused by the
         # timed steps like the tree; e2e builds them inside every step)
-        cfg["visibility_map"] = {"setting": args.vismap, "build_ms": map_build_ms,
+        run["visibility_map"] = {"setting": args.vismap, "build_ms": t["map_build_ms"],
                                  "cells_per_face_edge": int(res.stats["map_res"]),
                                  "bytes": int(res.stats["map_bytes"]),
                                  "entries_read_per_segment":
                                      agg["map_entries"] / max(1, agg["segments"]),
                                  "shadow_queries_per_segment":
                                      agg["shadow_queries"] / max(1, agg["segments"])}
-        cfg["rays_per_s"] = agg["rays"] / (total_ms / 1000.0) * world
         line = {
             "metric": "ray-bounce segments/s", "value": value, "unit": "segments/s",
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-            "config": cfg,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": traffic,
-                         "peak_source": src, "kernel": "trace_kernel<false>",
-                         "algorithmic_bytes_per_launch": per_launch,
-                         "kernel_ms_per_launch": kern_ms / args.steps},
+            "config": _config(w, args),
+            "adjoint_ratio": adj["ratio"] if adj else None,
+            "accuracy": acc,
+            "roofline": roof,
             "e2e": e2e,
-            "adjoint": adj,
-            "batched": bat,
-            "auralisation": aur,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clk,
+            "run": run,
+            "relief_hall": relief,
+            "adjoint": adj,
+            "batched": bat,
+            "auralisation": aur,
             "wall_s": wall,
         }
         print(json.dumps(line))
@@ -705,7 +845,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="relief_hall", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="cathedral", choices=sorted(WORKLOADS))
     ap.add_argument("--rays", type=int, default=None, help="rays per band (default: the config's)")
     ap.add_argument("--cpu-rays", type=int, default=None)
     ap.add_argument("--exact", action="store_true")
@@ -720,6 +860,15 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-aural", action="store_true")
+    ap.add_argument("--no-relief", action="store_true",
+                    help="skip the relief-hall object beside the headline workload")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-rays", type=int, default=1_000_000,
+                    help="rays per band of the fast-vs-exact accuracy renders")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--batch-curve", default="2000,20000,200000",
+                    help="rays per pair-frame of the batched crossover curve (one pair-frame "
+                         "per source/listener pair, keyframe 0); empty to skip")
     ap.add_argument("--aural-only", action="store_true",
                     help="run only the auralisation leg and print its object")
     ap.add_argument("--batch-rays", type=int, default=2000,

@@ -97,3 +97,36 @@ def edc_db_torch(h, floor_db: float = -300.0):
     tail = torch.flip(torch.cumsum(torch.flip(e, [-1]), -1), [-1])
     tot = tail[..., :1].clamp_min(1e-300)
     return torch.clamp(10.0 * torch.log10((tail / tot).clamp_min(1e-300)), min=floor_db)
+
+
+def track_t60_alone(h: np.ndarray, first: int, last: int) -> float:
+    """RecorderTrack::T60 of one track after the post-processing of
+    `EAR calc T60` (Power(0.335), truncation at max / 256) applied to that
+    track alone."""
+    t = np.ascontiguousarray(np.asarray(h, np.float32).copy())
+    new_last = power_and_truncate([t], [int(first)], [int(last)], [1])
+    return track_t60(t, int(first), int(new_last[0]))
+
+
+def fast_exact_accuracy(fast, exact, floor_db: float = -40.0) -> dict:
+    """Agreement of two renders of the same rays (``RenderResult``s with
+    host histograms): the largest difference of any track's per-band
+    Schroeder EDC down to ``floor_db`` (in the second render), and the
+    largest relative T60 difference over tracks and bands."""
+    hf, he = np.asarray(fast.hist), np.asarray(exact.hist)
+    edc_max, t60_rel, worst = 0.0, 0.0, None
+    for t in range(he.shape[0]):
+        for b in range(3):
+            if not he[t, b].any():
+                continue
+            ef, ee = edc_db(hf[t, b]), edc_db(he[t, b])
+            m = ee > floor_db
+            d = float(np.abs(ef[m] - ee[m]).max()) if m.any() else 0.0
+            if d > edc_max:
+                edc_max, worst = d, (t, b)
+            tf = track_t60_alone(hf[t, b], fast.first_sample[t, b], fast.last_sample[t, b])
+            te = track_t60_alone(he[t, b], exact.first_sample[t, b], exact.last_sample[t, b])
+            if te > 0:
+                t60_rel = max(t60_rel, abs(tf - te) / te)
+    return {"edc_max_db": edc_max, "t60_rel": t60_rel, "edc_floor_db": floor_db,
+            "worst_track_band": worst}
