@@ -40,7 +40,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr"] + ARCH 
 CUDA_UNITS = [
     ("bvh_build.cu", ["--fmad=false"]),
     ("trace_exact.cu", ["--fmad=false"]),
-    ("trace_fast.cu", ["--fmad=true"]),
+    ("trace_fast.cu", ["--fmad=true", "-prec-div=false"]),
     ("api.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
     ("vismap.cu", ["--fmad=false"]),

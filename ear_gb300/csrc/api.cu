@@ -167,7 +167,7 @@ __global__ void k_finalize(const FinalizeArgs f) {
     const float len = length(dist);
     const V3 dir = normalized(dist);
     const float amp = inv_sphere_2(len) * powf_portable(f.air[band], len) * f.dry;
-    const SplatPlan p = record_plan(R, band, dir, amp, len / 343.0f, len);
+    const SplatPlan p = record_plan<false>(R, band, dir, amp, len / 343.0f, len);
     for (int k = 0; k < p.tracks; ++k) {
       const int tb = (R.track0 + k) * 3 + band;
       float* row = f.hist + (size_t)tb * f.stride;
@@ -516,10 +516,10 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
       for (int k = 0; k < 3; ++k) locs[i][k] = recs[i].location[k];
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
-    // build peak: 24 bytes per entry for the sort plus the 8 kept; the
+    // build peak: 24 bytes per entry for the sort plus the 48 kept; the
     // automatic setting keeps at most EAR_VISMAP_AUTO_MAX_ENTRIES and
     // lowers the resolution by a quarter until the lists fit
-    const uint64_t fit = (uint64_t)(free_b / 2) / 32;
+    const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes);
     const uint64_t limit = std::min<uint64_t>(
         automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
     char msg[256] = "";

@@ -164,7 +164,7 @@ ear_status build_batch_maps(ear_batch* b) {
     if (use) {
       size_t free_b = 0, total_b = 0;
       CU(cudaMemGetInfo(&free_b, &total_b));
-      const uint64_t fit = (uint64_t)(free_b / 2) / 32;
+      const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes);
       const uint64_t limit = std::min<uint64_t>(
           automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
       char msg[256] = "";

@@ -102,7 +102,7 @@ struct __align__(16) SceneRef {
   // listener visibility maps of the recorders (vis_res = 0: none); a cell
   // holding more than vis_cap entries is left to the tree traversal
   const uint32_t* vis_start;
-  const int2* vis_entries;
+  const float4* vis_entries;  // kVisEntryVecs float4 per entry
   int vis_res;
   int vis_cap;
 };
@@ -159,7 +159,7 @@ struct TraceArgs {
   int* direct_vis;   // [recorder] direct-path visibility, or null
   // listener visibility maps of a single render's recorders (as in SceneRef)
   const uint32_t* vis_start;
-  const int2* vis_entries;
+  const float4* vis_entries;
   int vis_res;
   int vis_cap;
   // adjoint mode: upstream gradient of the raw splat sums [track][band][stride]
@@ -214,9 +214,16 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
 // of the triangles whose padded box meets the cell's cone of directions,
 // nearest first.  Cell index: ((recorder * 6 + face) * res + iv) * res + iu,
 // face = 2 * major axis + (major component < 0).
+// A visibility-list entry carries its triangle's test data inline, so a
+// walk reads one array: float4 (v0, distance bits of the padded box from
+// the recorder), float4 (e1 = v1 - v0, leaf position bits), float4 (e2 =
+// v2 - v0, 0) -- the same floats as the triangle record, so the test gives
+// the same result as the tree's.
+constexpr int kVisEntryVecs = 3;
+constexpr size_t kVisEntryBytes = sizeof(float) * 4 * kVisEntryVecs;
 struct VisMap {
   uint32_t* start = nullptr;
-  int2* entries = nullptr;
+  float4* entries = nullptr;
   int res = 0;
   int num_recs = 0;
   uint64_t num_entries = 0;

@@ -143,6 +143,21 @@ EAR_HD float powf_portable(float x, float y) {
   return (q * u2f((uint32_t)(ni + 64 + 127) << 23)) * 5.42101086e-20f;
 }
 
+// x^y in the kernels: powf_portable, or -- in the fast kernels
+// (FAST = true, device code) -- exp2(y log2 x) on the special-function unit,
+// a few ulp from it: statistically identical, not bit-identical.  y = 0 and
+// x = 1 give 1 as powf_portable does; the bases on this path are >= 0.
+template <bool FAST>
+EAR_HD float pow_sel(float x, float y) {
+#ifdef __CUDA_ARCH__
+  if (FAST) {
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    return exp2f(y * __log2f(x));
+  }
+#endif
+  return powf_portable(x, y);
+}
+
 // Philox-4x32-10 (Salmon et al., "Parallel random numbers: as easy as
 // 1, 2, 3", SC'11).
 struct U4 {

@@ -40,6 +40,15 @@ namespace EAR_NS {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// The fast kernels (trace_fast.cu, EAR_FAST_MATH) use the special-function
+// unit for powers and are compiled with approximate division; the exact
+// kernels keep IEEE operations throughout.
+#ifdef EAR_FAST_MATH
+constexpr bool kFastMath = true;
+#else
+constexpr bool kFastMath = false;
+#endif
+
 // Relative widening of the t-range culling (2^-16, about 128 ulp of t):
 // the slab distances and the triangle test round independently, so a box
 // whose entry distance rounds just above the current best hit must not be
@@ -466,8 +475,10 @@ __device__ __forceinline__ bool sample_dir(const TraceArgs& a, uint32_t ctx, uin
 // s .. s+w-1 (src/MonoRecorder.cpp:90-93), skipping negative positions
 // (src/StereoRecorder.cpp:93) and positions beyond the window, and updates
 // the FloatBuffer bookkeeping (first_sample / real_length,
-// src/Recorder.cpp:56-57) in shared memory.  Groups of four aligned bins go
-// out as one 16-byte vector reduction.
+// src/Recorder.cpp:56-57) in shared memory.  The values follow the
+// reference's float recurrence (one subtraction per position, skipped
+// positions included); they are added four aligned bins at a time, one
+// 16-byte vector reduction per group.
 __device__ __forceinline__ void splat(float* row, int* first, int* last, int nb, long long s,
                                       int w, float ampl, float step, uint32_t& bins) {
   bins += (uint32_t)w;
@@ -482,27 +493,24 @@ __device__ __forceinline__ void splat(float* row, int* first, int* last, int nb,
   if (lp > *(volatile int*)last) atomicMax(last, lp);
   if (firstpos >= nb) return;
   float v = ampl;
-  float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  int grp = -1;
-  for (int i = 0; i < w; ++i) {
-    const long long pos = s + i;
-    if (pos >= nb) break;
-    if (pos >= 0) {
-      const int g = (int)(pos >> 2);
-      if (g != grp) {
-        if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(row + 4 * grp), acc);
-        acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        grp = g;
-      }
-      const int c = (int)(pos & 3);
-      acc.x = c == 0 ? v : acc.x;
-      acc.y = c == 1 ? v : acc.y;
-      acc.z = c == 2 ? v : acc.z;
-      acc.w = c == 3 ? v : acc.w;
-    }
-    v -= step;
+  for (long long q = s; q < 0; ++q) v -= step;  // positions before the track
+  const int p0 = fp;                             // first and last position added
+  const int p1 = lastpos < nb ? (int)lastpos : nb - 1;
+  for (int g = p0 >> 2; g <= (p1 >> 2); ++g) {
+    const int q = 4 * g;
+    float4 acc;
+    const bool i0 = q >= p0 && q <= p1, i1 = q + 1 >= p0 && q + 1 <= p1;
+    const bool i2 = q + 2 >= p0 && q + 2 <= p1, i3 = q + 3 >= p0 && q + 3 <= p1;
+    acc.x = i0 ? v : 0.0f;
+    v = i0 ? v - step : v;
+    acc.y = i1 ? v : 0.0f;
+    v = i1 ? v - step : v;
+    acc.z = i2 ? v : 0.0f;
+    v = i2 ? v - step : v;
+    acc.w = i3 ? v : 0.0f;
+    v = i3 ? v - step : v;
+    atomicAdd(reinterpret_cast<float4*>(row + q), acc);
   }
-  if (grp >= 0) atomicAdd(reinterpret_cast<float4*>(row + 4 * grp), acc);
 }
 
 // Adjoint counterpart of splat(): the dot product of the upstream gradient
@@ -525,7 +533,7 @@ template <int MODE>
 __device__ __forceinline__ float record(const TraceArgs& a, const DevRecorder& R, int band, V3 dir,
                                         float amp, float t, float dist, int* s_first, int* s_last,
                                         uint32_t& bins) {
-  const SplatPlan p = record_plan(R, band, dir, amp, t, dist);
+  const SplatPlan p = record_plan<kFastMath>(R, band, dir, amp, t, dist);
   float G = 0.0f;
   for (int k = 0; k < p.tracks; ++k) {
     const int tb = (R.track0 + k) * 3 + band;
@@ -603,42 +611,45 @@ struct Vertex {
   bool conn;     // connect the recorders at this vertex
 };
 
+// Cell of the direction o - location (sdir = location - o) in list set mi
+// of the scene's maps; false for a degenerate direction.
+__device__ __forceinline__ bool vis_cell_of(const SceneRef& S, int mi, V3 sdir, uint32_t& cell) {
+  int f, iu, iv;
+  const int res = S.vis_res;
+  if (!vis_query_cell(sdir.x, sdir.y, sdir.z, res, f, iu, iv)) return false;
+  cell = ((uint32_t)(mi * 6 + f) * (uint32_t)res + (uint32_t)iv) * (uint32_t)res + (uint32_t)iu;
+  return true;
+}
+
 // Visibility test of the segment from `o` to the recorder with list set
 // `ri` in the scene's maps (sdir = its location - o, len = |sdir|): the
 // entries of the cell of direction o - location nearer than the vertex, each
-// by the tree's own leaf test.  Returns 1 blocked, 0 clear, -1 when the map
-// leaves the test to the tree (degenerate direction, or a cell longer than
-// vis_cap).  The result equals the tree traversal's: the entries are every
-// triangle whose padded box meets the segment.
+// by the tree's own triangle test.  Returns 1 blocked, 0 clear, -1 when the
+// map leaves the test to the tree (degenerate direction, or a cell longer
+// than vis_cap).  The result equals the tree traversal's: the entries are
+// every triangle whose padded box meets the segment.
 __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 sdir, float len,
                                             LaneCounters& c, int& err) {
-  int f, iu, iv;
-  const int res = S.vis_res;
-  if (!vis_query_cell(sdir.x, sdir.y, sdir.z, res, f, iu, iv)) return -1;
-  const uint32_t cell =
-      ((uint32_t)(ri * 6 + f) * (uint32_t)res + (uint32_t)iv) * (uint32_t)res + (uint32_t)iu;
+  uint32_t cell;
+  if (!vis_cell_of(S, ri, sdir, cell)) return -1;
   const uint32_t b = __ldg(S.vis_start + cell), e = __ldg(S.vis_start + cell + 1);
   if (e - b > (uint32_t)S.vis_cap) return -1;
   // entries are ordered by their boxes' distance from the recorder; a hit
   // point of the segment lies nearer than len (t > 1e-5)
   const float cut = vis_cut(len);
-  // two entries per step: both triangles' loads are in flight before the
-  // first test (Mesh::LineIntersection: 1e-5 < t < 1, src/Mesh.cpp:65)
+  // two entries per step, both loaded before the first test; each carries
+  // its triangle's test data, so one array is read (Mesh::LineIntersection:
+  // 1e-5 < t < 1, src/Mesh.cpp:65)
   uint32_t i = b;
   bool blocked = false;
   while (i < e) {
-    const int2 e0 = __ldg(S.vis_entries + i);
+    const float4* E0 = S.vis_entries + (size_t)kVisEntryVecs * i;
     const bool has1 = i + 1 < e;
-    const int2 e1 = has1 ? __ldg(S.vis_entries + i + 1) : e0;
-    if (__int_as_float(e0.y) > cut) break;
-    const bool use1 = has1 && __int_as_float(e1.y) <= cut;
-    const int p0 = clamp_index(e0.x, S.num_tris, err);
-    const int p1 = use1 ? clamp_index(e1.x, S.num_tris, err) : p0;
-    float4 A0, B0, A1, B1;
-    ldg256(S.tris + 4 * p0, A0, B0);
-    const float4 C0 = __ldg(S.tris + 4 * p0 + 2);
-    ldg256(S.tris + 4 * p1, A1, B1);
-    const float4 C1 = __ldg(S.tris + 4 * p1 + 2);
+    const float4* E1 = has1 ? E0 + kVisEntryVecs : E0;
+    const float4 A0 = __ldg(E0), B0 = __ldg(E0 + 1), C0 = __ldg(E0 + 2);
+    const float4 A1 = __ldg(E1), B1 = __ldg(E1 + 1), C1 = __ldg(E1 + 2);
+    if (A0.w > cut) break;
+    const bool use1 = has1 && A1.w <= cut;
     float t;
     ++c.tris;
     ++i;
@@ -698,18 +709,18 @@ __device__ __forceinline__ int connect_one(const TraceArgs& a, const SceneRef* s
       const float diff_factor = -dot(n, st.prev);
       const float rv = dot(refl_vector, lsdir);
       const float spec_factor = (0.0f < rv) ? rv : 0.0f;
-      factor = vx.spec * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+      factor = vx.spec * 1001.0f * pow_sel<kFastMath>(spec_factor, 1000.0f) +
                (1.0f - vx.spec) * diff_factor;
     } else {
       const float diff_factor = dot(n, st.prev);
       const float rv = dot(st.prev, lsdir);
       const float spec_factor = (0.0f < rv) ? rv : 0.0f;
-      factor = vx.spec * 1001.0f * powf_portable(spec_factor, 1000.0f) +
+      factor = vx.spec * 1001.0f * pow_sel<kFastMath>(spec_factor, 1000.0f) +
                (1.0f - vx.spec) * diff_factor;
     }
     I *= factor;
   }
-  I *= powf_portable(a.air[st.band], len);
+  I *= pow_sel<kFastMath>(a.air[st.band], len);
   I *= inv_hemi_2(len);
   if (!invalid_float(I)) {
     if (k & 1) I *= -1.0f;
@@ -856,7 +867,7 @@ __device__ bool bounce_vertex(const TraceArgs& a, const DevMaterial* __restrict_
   const float om = 1.0f - spec;
   v = normalized(mk(v.x * om + base.x * spec, v.y * om + base.y * spec, v.z * om + base.z * spec));
   const float l = length(sub(p, st.o));
-  st.I *= powf_portable(a.air[band], l);
+  st.I *= pow_sel<kFastMath>(a.air[band], l);
   st.L += l;
   st.o = p;
   st.d = v;

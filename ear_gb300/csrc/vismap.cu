@@ -218,11 +218,21 @@ __global__ void k_vis_start(const uint64_t* __restrict__ keys, int64_t n, uint64
   start[c] = (uint32_t)lo;
 }
 
+// Entry i: the triangle at leaf position vals[i] with its test data inline
+// (kVisEntryVecs float4, see VisMap) and the distance of keys[i].
 __global__ void k_vis_pack(const uint64_t* __restrict__ keys, const int32_t* __restrict__ vals,
-                           int64_t n, int2* __restrict__ entries) {
+                           int64_t n, const float4* __restrict__ tris, int num_tris,
+                           float4* __restrict__ entries) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  entries[i] = make_int2(vals[i], (int)(uint32_t)keys[i]);
+  const int pos = vals[i];
+  const int q = (unsigned)pos < (unsigned)num_tris ? pos : 0;
+  const float4 A = __ldg(tris + 4 * (size_t)q), B = __ldg(tris + 4 * (size_t)q + 1),
+               C = __ldg(tris + 4 * (size_t)q + 2);
+  float4* E = entries + (size_t)kVisEntryVecs * (size_t)i;
+  E[0] = make_float4(A.x, A.y, A.z, __uint_as_float((uint32_t)keys[i]));
+  E[1] = make_float4(B.x, B.y, B.z, __int_as_float(pos));
+  E[2] = make_float4(C.x, C.y, C.z, 0.0f);
 }
 
 int bits_for(uint64_t v) {
@@ -331,18 +341,19 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
     tmp_bytes = need;
     VCK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, dk, dv, (int)n, 0, end_bit, st));
     VCK(cudaMalloc(&out->start, sizeof(uint32_t) * (cells + 1)));
-    VCK(cudaMalloc(&out->entries, sizeof(int2) * std::max<int64_t>(n, 1)));
+    VCK(cudaMalloc(&out->entries, kVisEntryBytes * (size_t)std::max<int64_t>(n, 1)));
     k_vis_start<<<(unsigned)((cells + 1 + B - 1) / B), B, 0, st>>>(dk.Current(), n, cells, out->start);
     VCK(cudaGetLastError());
     if (n > 0) {
-      k_vis_pack<<<(unsigned)((n + B - 1) / B), B, 0, st>>>(dk.Current(), dv.Current(), n, out->entries);
+      k_vis_pack<<<(unsigned)((n + B - 1) / B), B, 0, st>>>(dk.Current(), dv.Current(), n, s.tris,
+                                                             (int)s.num_tris, out->entries);
       VCK(cudaGetLastError());
     }
     VCK(cudaStreamSynchronize(st));
     out->res = res;
     out->num_recs = nrec;
     out->num_entries = (uint64_t)n;
-    out->bytes = sizeof(uint32_t) * (cells + 1) + sizeof(int2) * (size_t)n;
+    out->bytes = sizeof(uint32_t) * (cells + 1) + kVisEntryBytes * (size_t)n;
   }
 done:
   cudaFree(count);

@@ -188,8 +188,14 @@ EAR_VIS_HD bool vis_query_cell(float sx, float sy, float sz, int res, int& f, in
     v = qy;
   }
   if (!(m > 0.0f)) return false;
+#ifdef __CUDA_ARCH__
+  // correctly rounded even where a unit is compiled with approximate division
+  iu = vis_cell(__fdiv_rn(u, m), res);
+  iv = vis_cell(__fdiv_rn(v, m), res);
+#else
   iu = vis_cell(u / m, res);
   iv = vis_cell(v / m, res);
+#endif
   return true;
 }
 

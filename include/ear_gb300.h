@@ -144,7 +144,7 @@ typedef struct ear_bvh_opts {
   int32_t reserved;
 } ear_bvh_opts;
 
-#define EAR_VISMAP_AUTO_MAX_ENTRIES (1ull << 30) /* 8 GiB of lists */
+#define EAR_VISMAP_AUTO_MAX_ENTRIES (1ull << 30) /* 48 GiB of lists (48 B per entry) */
 
 #define EAR_BVH_DEFAULT 0
 #define EAR_BVH_LBVH 1

@@ -184,3 +184,42 @@ def test_batch_with_maps_equals_plain_renders_without():
             e2 = (np.asarray(p.hist, np.float64) ** 2).sum(-1)
             assert (np.abs(e1 - e2) <= 1e-5 * np.maximum(e2, 1e-30)).all(), i
         b.close()
+
+
+def _grazing_room():
+    """A 20 x 20 x 4 m box of 12 large triangles (and a 5 cm step) whose
+    recorders sit 0.1 to 2 mm above the floor and 0.1 mm from a wall: the
+    segments from path
+    vertices on the floor and that wall to them graze the large triangles'
+    planes (cosines down to about 1e-5), where the triangle test's own
+    rounding decides near-zero crossings."""
+    w = scenes.shoebox()
+    # the room and a 5 cm step on its floor (occludes some grazing segments)
+    step = scenes.box_triangles(4.0, 3.0, 0.05) + np.tile(np.array([6.0, 8.0, 0.0], np.float32), 3)
+    v = np.concatenate([scenes.box_triangles(20.0, 20.0, 4.0), step], 0).astype(np.float32)
+    recs = [Recorder(location=np.array(p, np.float32)) for p in
+            [(10.0, 10.0, 0.0001), (3.0, 15.0, 0.0005), (17.0, 4.0, 0.002), (0.0001, 10.0, 1.5),
+             (15.0, 15.0, 0.0001)]]
+    return dataclasses.replace(w, vertices=v, material_ids=np.zeros(len(v), np.int32),
+                               recorders=recs, name="grazing-box",
+                               render=dict(w.render, num_bins=88200))
+
+
+def test_grazing_segments_bit_exact_maps_on_off_and_oracle():
+    w = _grazing_room()
+    nrays, max_record, band = 3000, 40, 1
+    off = _debug(w, -1, nrays, max_record, band)
+    kw = dict(w.render, num_rays=nrays, bands=(band,))
+    ref = oracle.render(w.vertices, w.material_ids, w.materials, w.source, w.recorders,
+                        threads=THREADS, debug_band=band, debug_rays=nrays,
+                        debug_max_record=max_record, **kw)
+    for a, b in zip(off, ref["debug"]):
+        np.testing.assert_array_equal(a, b)
+    for res in (8, 64, 256):
+        on = _debug(w, res, nrays, max_record, band)
+        for a, b in zip(off, on):
+            np.testing.assert_array_equal(a, b)
+    # the floor's recorders are seen from some vertices and hidden from others
+    full = (1 << len(w.recorders)) - 1
+    vis = off[2][off[0] >= 0] & full
+    assert (vis != 0).any() and (vis != full).any()
