@@ -81,20 +81,22 @@ __device__ __forceinline__ Ray make_ray(V3 o, V3 d) {
   return r;
 }
 
-// Slab test against [lo, hi] for t in [0, tmax] (tmax > 0); conservative
-// only.  The entry distance tn = max(min x, min y, min z, 0) and exit
-// distance tf = min(max x, max y, max z, tmax) use 3-input integer min/max
+// Slab test against [lo, hi] for t in [tmin, tmax] (0 <= tmin < tmax, tmin
+// given by its bits); conservative only.  The entry distance tn = max(min
+// x, min y, min z, tmin) and exit distance tf = min(max x, max y, max z,
+// tmax) use 3-input integer min/max
 // on the float bit patterns: signed-integer order equals float order among
 // non-negative floats and puts every negative float below them, so the
 // relu max gives tn exactly, and tf, which is only compared with tn >= 0,
 // keeps its sign.
 __device__ __forceinline__ bool box_hit(float lx, float hx, float ly, float hy, float lz, float hz,
-                                        const Ray& r, float tmax, float& tnear) {
+                                        const Ray& r, float tmax, int tmin_bits, float& tnear) {
   const float tx0 = __fmaf_rn(lx, r.ix, r.nx), tx1 = __fmaf_rn(hx, r.ix, r.nx);
   const float ty0 = __fmaf_rn(ly, r.iy, r.ny), ty1 = __fmaf_rn(hy, r.iy, r.ny);
   const float tz0 = __fmaf_rn(lz, r.iz, r.nz), tz1 = __fmaf_rn(hz, r.iz, r.nz);
-  const int tn = __vimax3_s32_relu(__float_as_int(fminf(tx0, tx1)), __float_as_int(fminf(ty0, ty1)),
-                                   __float_as_int(fminf(tz0, tz1)));
+  const int tn = __vimax3_s32(__vimax_s32_relu(__float_as_int(fminf(tx0, tx1)),
+                                               __float_as_int(fminf(ty0, ty1))),
+                              __float_as_int(fminf(tz0, tz1)), tmin_bits);
   const int tf = __vimin3_s32(__float_as_int(fmaxf(tx0, tx1)), __float_as_int(fmaxf(ty0, ty1)),
                               __float_as_int(fminf(fmaxf(tz0, tz1), tmax)));
   tnear = __int_as_float(tn);
@@ -228,6 +230,11 @@ __device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
   h.orig = INT_MAX;
   if (S.num_tris == 0) return false;
   const Ray r = make_ray(o, d);
+  // closest hit: only t > 0.001 counts (src/Mesh.cpp:40), so boxes the
+  // ray leaves before 0.001 - slack hold no hit (slack = the boxes' padding
+  // covers the rounding of the slab distances, as on the far side); the
+  // boxes around the ray's origin on its surface are culled at once
+  const int tmin_bits = ANY ? 0 : __float_as_int(fmaxf(0.001f - slack, 0.0f));
   int cur = 0;
   unsigned long long trail = 1ull;
   int iters = 0;
@@ -248,8 +255,8 @@ __device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     const int4 ch = as_int4(nd4);
     const float lim = ANY ? tlimit + slack : h.t + (h.t * kSlackRel + slack);
     float t0, t1;
-    bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, t0);
-    bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, t1);
+    bool h0 = box_hit(na.x, na.y, na.z, na.w, nb.x, nb.y, r, lim, tmin_bits, t0);
+    bool h1 = box_hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, r, lim, tmin_bits, t1);
     // the hit leaf children (0, 1 or 2) are tested by one loop, so lanes
     // with one leaf and lanes with two share the same instructions
     const bool l0 = h0 && ch.x < 0, l1 = h1 && ch.y < 0;
@@ -326,6 +333,11 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
   h.orig = INT_MAX;
   if (S.num_tris == 0) return false;
   const Ray r = make_ray(o, d);
+  // closest hit: only t > 0.001 counts (src/Mesh.cpp:40), so boxes the
+  // ray leaves before 0.001 - slack hold no hit (slack = the boxes' padding
+  // covers the rounding of the slab distances, as on the far side); the
+  // boxes around the ray's origin on its surface are culled at once
+  const int tmin_bits = ANY ? 0 : __float_as_int(fmaxf(0.001f - slack, 0.0f));
   const Node4* __restrict__ nodes = S.nodes4;
   int cur = 0;
   unsigned long long tlo = 0ull, thi = 0ull;  // the trail
@@ -356,7 +368,7 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     for (int k = 0; k < 4; ++k) {
       float tn;
       const bool b = box_hit(lane4(lx, k), lane4(hx, k), lane4(ly, k), lane4(hy, k), lane4(lz, k),
-                             lane4(hz, k), r, lim, tn);
+                             lane4(hz, k), r, lim, tmin_bits, tn);
       tk[k] = tn;
       if (((cand >> k) & 1u) && b) hit |= 1u << k;
       if (lane4(ch, k) < 0) leaf |= 1u << k;
