@@ -65,8 +65,9 @@ struct Ray {
 };
 
 __device__ __forceinline__ float safe_inv(float d) {
-  // 1/d with zero components replaced by +-1e-30 so slabs stay finite.
-  const float dd = (d != 0.0f) ? d : copysignf(1e-30f, d);
+  // 1/d with components below 1e-30 in magnitude (zero included) replaced
+  // by +-1e-30, so slabs stay finite and 1/d keeps d's sign.
+  const float dd = (fabsf(d) >= 1e-30f) ? d : copysignf(1e-30f, d);
   return 1.0f / dd;
 }
 
@@ -99,6 +100,24 @@ __device__ __forceinline__ bool box_hit(float lx, float hx, float ly, float hy, 
                               __float_as_int(fminf(tz0, tz1)), tmin_bits);
   const int tf = __vimin3_s32(__float_as_int(fmaxf(tx0, tx1)), __float_as_int(fmaxf(ty0, ty1)),
                               __float_as_int(fminf(fmaxf(tz0, tz1), tmax)));
+  tnear = __int_as_float(tn);
+  return tn <= tf;
+}
+
+// The same test with each axis's near and far plane chosen by the sign of
+// the ray's direction (the octant): the plane nearer along the ray is the
+// low one for a positive direction, the high one for a negative, so the
+// slab distances need no per-axis min / max.  Equal to box_hit's
+// distances, which take that min / max of the same two values.
+__device__ __forceinline__ bool box_hit_nf(float nx, float fx, float ny, float fy, float nz, float fz,
+                                           const Ray& r, float tmax, int tmin_bits, float& tnear) {
+  const float a = __fmaf_rn(nx, r.ix, r.nx), b = __fmaf_rn(ny, r.iy, r.ny);
+  const float c = __fmaf_rn(nz, r.iz, r.nz);
+  const float x = __fmaf_rn(fx, r.ix, r.nx), y = __fmaf_rn(fy, r.iy, r.ny);
+  const float z = __fmaf_rn(fz, r.iz, r.nz);
+  const int tn = __vimax3_s32(__float_as_int(a), __float_as_int(b),
+                              max(__float_as_int(c), tmin_bits));
+  const int tf = __vimin3_s32(__float_as_int(x), __float_as_int(y), __float_as_int(fminf(z, tmax)));
   tnear = __int_as_float(tn);
   return tn <= tf;
 }
@@ -354,10 +373,15 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     cur = clamp_index(cur, S.num_nodes, err);
     const Node4* nd = nodes + cur;
     c.nodes += 2;  // two 64-byte halves
-    float4 lx, hx, ly, hy, lz, hz, chf, mtf;
-    ldg256(&nd->lox, lx, hx);
-    ldg256(&nd->loy, ly, hy);
-    ldg256(&nd->loz, lz, hz);
+    // the near and far planes of each axis, picked by the load address
+    // (lox, hix, loy, hiy, loz, hiz are consecutive float4s)
+    const float4* P = &nd->lox;
+    const int sx = __float_as_int(r.ix) < 0, sy = __float_as_int(r.iy) < 0,
+              sz = __float_as_int(r.iz) < 0;
+    const float4 nx4 = __ldg(P + sx), fx4 = __ldg(P + 1 - sx);
+    const float4 ny4 = __ldg(P + 2 + sy), fy4 = __ldg(P + 3 - sy);
+    const float4 nz4 = __ldg(P + 4 + sz), fz4 = __ldg(P + 5 - sz);
+    float4 chf, mtf;
     ldg256(&nd->child, chf, mtf);
     const int4 ch = as_int4(chf), meta = as_int4(mtf);
     const unsigned cand = (reentry ? (unsigned)(tlo & 0xFull) : 0xFu) & (unsigned)meta.y;
@@ -367,8 +391,8 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       float tn;
-      const bool b = box_hit(lane4(lx, k), lane4(hx, k), lane4(ly, k), lane4(hy, k), lane4(lz, k),
-                             lane4(hz, k), r, lim, tmin_bits, tn);
+      const bool b = box_hit_nf(lane4(nx4, k), lane4(fx4, k), lane4(ny4, k), lane4(fy4, k),
+                                lane4(nz4, k), lane4(fz4, k), r, lim, tmin_bits, tn);
       tk[k] = tn;
       if (((cand >> k) & 1u) && b) hit |= 1u << k;
       if (lane4(ch, k) < 0) leaf |= 1u << k;
