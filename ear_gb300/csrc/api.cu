@@ -490,7 +490,7 @@ uint64_t vis_map_key(const ear_scene* s, const ear_recorder* recs, int32_t nrec,
 }
 
 void set_vis_args(const ear_scene* s, TraceArgs& a) {
-  a.vis_start = s->vis.start;
+  a.vis_cells = s->vis.cells;
   a.vis_entries = s->vis.entries;
   a.vis_res = s->vis.res;
   a.vis_cap = kVisWalkCap;
@@ -519,7 +519,7 @@ ear_status use_visibility_maps(ear_scene* s, const ear_recorder* recs, int32_t n
     // build peak: 24 bytes per entry for the sort plus the 48 kept; the
     // automatic setting keeps at most EAR_VISMAP_AUTO_MAX_ENTRIES and
     // lowers the resolution by a quarter until the lists fit
-    const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes);
+    const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes + kVisCellBytes);
     const uint64_t limit = std::min<uint64_t>(
         automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
     char msg[256] = "";
@@ -1198,7 +1198,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.dbg_band = -1;
   // listener visibility maps an earlier ear_render built for this recorder
   // set are read; none is built here (a build allocates)
-  if (nrec > 0 && s->vis_opt >= 0 && s->vis_valid && !s->vis_refused && s->vis.start) {
+  if (nrec > 0 && s->vis_opt >= 0 && s->vis_valid && !s->vis_refused && s->vis.cells) {
     const int res = s->vis_opt > 0 ? s->vis_opt : vis_auto_res(s->ds.num_tris);
     if (vis_map_key(s, recs, nrec, res) == s->vis_key) set_vis_args(s, a);
   }

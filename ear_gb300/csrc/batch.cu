@@ -104,9 +104,9 @@ SceneRef scene_ref(const ear_scene* s, int mat_base, const VisMap& m) {
   r.mat_base = mat_base;
   r.num_mats = s->num_mats;
   r.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
-  r.vis_start = m.start;
+  r.vis_cells = m.cells;
   r.vis_entries = m.entries;
-  r.vis_res = m.start ? m.res : 0;
+  r.vis_res = m.cells ? m.res : 0;
   r.vis_cap = kVisWalkCap;
   return r;
 }
@@ -164,7 +164,7 @@ ear_status build_batch_maps(ear_batch* b) {
     if (use) {
       size_t free_b = 0, total_b = 0;
       CU(cudaMemGetInfo(&free_b, &total_b));
-      const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes);
+      const uint64_t fit = (uint64_t)(free_b / 2) / (24 + kVisEntryBytes + kVisCellBytes);
       const uint64_t limit = std::min<uint64_t>(
           automatic ? (uint64_t)EAR_VISMAP_AUTO_MAX_ENTRIES : (1ull << 31) - 1, fit);
       char msg[256] = "";
@@ -635,7 +635,7 @@ ear_status ear_batch_run(ear_batch* b, ear_render_stats* stats) {
     stats->map_build_ms = b->map_build_ms;
     for (const VisMap& m : b->maps) {
       stats->map_bytes += m.bytes;
-      stats->map_res = std::max(stats->map_res, m.start ? m.res : 0);
+      stats->map_res = std::max(stats->map_res, m.cells ? m.res : 0);
     }
   }
   b->map_build_ms = 0.0;

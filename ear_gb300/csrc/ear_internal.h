@@ -101,7 +101,7 @@ struct __align__(16) SceneRef {
   int any_far;  // visibility tests visit the farthest hit child first
   // listener visibility maps of the recorders (vis_res = 0: none); a cell
   // holding more than vis_cap entries is left to the tree traversal
-  const uint32_t* vis_start;
+  const float4* vis_cells;    // 2 float4 per cell (VisMap)
   const float4* vis_entries;  // kVisEntryVecs float4 per entry
   int vis_res;
   int vis_cap;
@@ -158,7 +158,7 @@ struct TraceArgs {
   int2* first_last;  // [track][band]
   int* direct_vis;   // [recorder] direct-path visibility, or null
   // listener visibility maps of a single render's recorders (as in SceneRef)
-  const uint32_t* vis_start;
+  const float4* vis_cells;
   const float4* vis_entries;
   int vis_res;
   int vis_cap;
@@ -221,8 +221,15 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
 // the same result as the tree's.
 constexpr int kVisEntryVecs = 3;
 constexpr size_t kVisEntryBytes = sizeof(float) * 4 * kVisEntryVecs;
+// A cell is two float4s, 32 bytes: (start bits, end bits, d0, d1) and
+// (d2, d3, d4, d5) -- its list's range in entries[] and the distances of
+// its first kVisCellDists entries (+inf past the list's end), so a walk
+// counts the entries it must test from the cell alone and reads no entry
+// just to find that it lies beyond the vertex.
+constexpr int kVisCellDists = 6;
+constexpr size_t kVisCellBytes = 32;
 struct VisMap {
-  uint32_t* start = nullptr;
+  float4* cells = nullptr;
   float4* entries = nullptr;
   int res = 0;
   int num_recs = 0;

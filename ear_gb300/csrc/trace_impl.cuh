@@ -623,7 +623,7 @@ __device__ __forceinline__ SceneRef scene_of(const TraceArgs& a, const SceneRef*
   S.mat_base = 0;
   S.num_mats = a.num_mats;
   S.traverse_budget = a.traverse_budget;
-  S.vis_start = a.vis_start;
+  S.vis_cells = a.vis_cells;
   S.vis_entries = a.vis_entries;
   S.vis_res = a.vis_res;
   S.vis_cap = a.vis_cap;
@@ -668,24 +668,34 @@ __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 
                                             LaneCounters& c, int& err) {
   uint32_t cell;
   if (!vis_cell_of(S, ri, sdir, cell)) return -1;
-  const uint32_t b = __ldg(S.vis_start + cell), e = __ldg(S.vis_start + cell + 1);
+  float4 H0, H1;
+  ldg256(S.vis_cells + 2 * (size_t)cell, H0, H1);
+  const uint32_t b = __float_as_uint(H0.x), e = __float_as_uint(H0.y);
   if (e - b > (uint32_t)S.vis_cap) return -1;
   // entries are ordered by their boxes' distance from the recorder; a hit
-  // point of the segment lies nearer than len (t > 1e-5)
+  // point of the segment lies nearer than len (t > 1e-5).  The cell holds
+  // the first six distances (+inf past the end): the entries to test among
+  // them are counted here, so none is read only to find it too far.
   const float cut = vis_cut(len);
+  const uint32_t known =
+      (uint32_t)(H0.z <= cut) + (uint32_t)(H0.w <= cut) + (uint32_t)(H1.x <= cut) +
+      (uint32_t)(H1.y <= cut) + (uint32_t)(H1.z <= cut) + (uint32_t)(H1.w <= cut);
+  // all six nearer: later entries may be too, and carry their distances
+  const uint32_t end = known == kVisCellDists ? e : b + known;
+  const bool check = known == kVisCellDists;
   // two entries per step, both loaded before the first test; each carries
   // its triangle's test data, so one array is read (Mesh::LineIntersection:
   // 1e-5 < t < 1, src/Mesh.cpp:65)
   uint32_t i = b;
   bool blocked = false;
-  while (i < e) {
+  while (i < end) {
     const float4* E0 = S.vis_entries + (size_t)kVisEntryVecs * i;
-    const bool has1 = i + 1 < e;
+    const bool has1 = i + 1 < end;
     const float4* E1 = has1 ? E0 + kVisEntryVecs : E0;
     const float4 A0 = __ldg(E0), B0 = __ldg(E0 + 1), C0 = __ldg(E0 + 2);
     const float4 A1 = __ldg(E1), B1 = __ldg(E1 + 1), C1 = __ldg(E1 + 2);
-    if (A0.w > cut) break;
-    const bool use1 = has1 && A1.w <= cut;
+    if (check && A0.w > cut) break;
+    const bool use1 = has1 && !(check && A1.w > cut);
     float t;
     ++c.tris;
     ++i;

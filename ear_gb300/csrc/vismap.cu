@@ -235,6 +235,20 @@ __global__ void k_vis_pack(const uint64_t* __restrict__ keys, const int32_t* __r
   E[2] = make_float4(C.x, C.y, C.z, 0.0f);
 }
 
+// Cell c: (start, end, the distances of its first kVisCellDists entries,
+// +inf past the end); start = the binary-searched first entries.
+__global__ void k_vis_cells(const uint32_t* __restrict__ start, const uint64_t* __restrict__ keys,
+                            uint64_t cells, float4* __restrict__ out) {
+  const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cells) return;
+  const uint32_t b = start[c], e = start[c + 1];
+  float d[kVisCellDists];
+  for (int k = 0; k < kVisCellDists; ++k)
+    d[k] = b + k < e ? __uint_as_float((uint32_t)keys[b + k]) : __int_as_float(0x7f800000);
+  out[2 * c] = make_float4(__uint_as_float(b), __uint_as_float(e), d[0], d[1]);
+  out[2 * c + 1] = make_float4(d[2], d[3], d[4], d[5]);
+}
+
 int bits_for(uint64_t v) {
   int b = 0;
   while (b < 64 && (v >> b)) ++b;
@@ -244,7 +258,7 @@ int bits_for(uint64_t v) {
 }  // namespace
 
 void free_vis_map(VisMap* m) {
-  cudaFree(m->start);
+  cudaFree(m->cells);
   cudaFree(m->entries);
   *m = VisMap{};
 }
@@ -267,6 +281,7 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
   cudaError_t rc = cudaSuccess;
   VisBuildArgs a = {};
   uint64_t *count = nullptr, *offset = nullptr, *keys = nullptr, *keys2 = nullptr;
+  uint32_t* start = nullptr;
   int32_t *vals = nullptr, *vals2 = nullptr;
   int64_t* big = nullptr;
   unsigned long long* d_num_big = nullptr;
@@ -340,9 +355,12 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
     VCK(cudaMalloc(&tmp, std::max<size_t>(need, 1)));
     tmp_bytes = need;
     VCK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, dk, dv, (int)n, 0, end_bit, st));
-    VCK(cudaMalloc(&out->start, sizeof(uint32_t) * (cells + 1)));
+    VCK(cudaMalloc(&start, sizeof(uint32_t) * (cells + 1)));
+    VCK(cudaMalloc(&out->cells, kVisCellBytes * (size_t)cells));
     VCK(cudaMalloc(&out->entries, kVisEntryBytes * (size_t)std::max<int64_t>(n, 1)));
-    k_vis_start<<<(unsigned)((cells + 1 + B - 1) / B), B, 0, st>>>(dk.Current(), n, cells, out->start);
+    k_vis_start<<<(unsigned)((cells + 1 + B - 1) / B), B, 0, st>>>(dk.Current(), n, cells, start);
+    VCK(cudaGetLastError());
+    k_vis_cells<<<(unsigned)((cells + B - 1) / B), B, 0, st>>>(start, dk.Current(), cells, out->cells);
     VCK(cudaGetLastError());
     if (n > 0) {
       k_vis_pack<<<(unsigned)((n + B - 1) / B), B, 0, st>>>(dk.Current(), dv.Current(), n, s.tris,
@@ -353,9 +371,10 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
     out->res = res;
     out->num_recs = nrec;
     out->num_entries = (uint64_t)n;
-    out->bytes = sizeof(uint32_t) * (cells + 1) + kVisEntryBytes * (size_t)n;
+    out->bytes = kVisCellBytes * (size_t)cells + kVisEntryBytes * (size_t)n;
   }
 done:
+  cudaFree(start);
   cudaFree(count);
   cudaFree(offset);
   cudaFree(big);
