@@ -221,13 +221,13 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
 // the same result as the tree's.
 constexpr int kVisEntryVecs = 3;
 constexpr size_t kVisEntryBytes = sizeof(float) * 4 * kVisEntryVecs;
-// A cell is two float4s, 32 bytes: (start bits, end bits, d0, d1) and
-// (d2, d3, d4, d5) -- its list's range in entries[] and the distances of
-// its first kVisCellDists entries (+inf past the list's end), so a walk
-// counts the entries it must test from the cell alone and reads no entry
-// just to find that it lies beyond the vertex.
-constexpr int kVisCellDists = 6;
-constexpr size_t kVisCellBytes = 32;
+// A cell is four float4s, 64 bytes: (start bits, end bits, d1, d2), then
+// its first entry (three float4s as in entries[], its distance d0 in the
+// first one's w; zeros and d0 = +inf for an empty list) -- so a walk counts
+// from the cell alone which of its first three entries lie nearer than the
+// vertex, and tests the first while the next ones load.
+constexpr int kVisCellDists = 3;
+constexpr size_t kVisCellBytes = 64;
 struct VisMap {
   float4* cells = nullptr;
   float4* entries = nullptr;

@@ -668,48 +668,48 @@ __device__ __forceinline__ int vis_map_test(const SceneRef& S, int ri, V3 o, V3 
                                             LaneCounters& c, int& err) {
   uint32_t cell;
   if (!vis_cell_of(S, ri, sdir, cell)) return -1;
-  float4 H0, H1;
-  ldg256(S.vis_cells + 2 * (size_t)cell, H0, H1);
-  const uint32_t b = __float_as_uint(H0.x), e = __float_as_uint(H0.y);
+  const float4* Cp = S.vis_cells + 4 * (size_t)cell;
+  float4 H, A0, B0, C0;
+  ldg256(Cp, H, A0);
+  ldg256(Cp + 2, B0, C0);
+  const uint32_t b = __float_as_uint(H.x), e = __float_as_uint(H.y);
   if (e - b > (uint32_t)S.vis_cap) return -1;
   // entries are ordered by their boxes' distance from the recorder; a hit
   // point of the segment lies nearer than len (t > 1e-5).  The cell holds
-  // the first six distances (+inf past the end): the entries to test among
-  // them are counted here, so none is read only to find it too far.
+  // the first three distances (+inf past the end) and the first entry: the
+  // entries to test among the first three are counted here, and the first
+  // is tested from the cell while the next ones load.
   const float cut = vis_cut(len);
-  const uint32_t known =
-      (uint32_t)(H0.z <= cut) + (uint32_t)(H0.w <= cut) + (uint32_t)(H1.x <= cut) +
-      (uint32_t)(H1.y <= cut) + (uint32_t)(H1.z <= cut) + (uint32_t)(H1.w <= cut);
-  // all six nearer: later entries may be too, and carry their distances
+  const uint32_t known = (uint32_t)(A0.w <= cut) + (uint32_t)(H.z <= cut) + (uint32_t)(H.w <= cut);
+  if (known == 0) return 0;
+  // all three nearer: later entries may be too, and carry their distances
   const uint32_t end = known == kVisCellDists ? e : b + known;
   const bool check = known == kVisCellDists;
-  // two entries per step, both loaded before the first test; each carries
-  // its triangle's test data, so one array is read (Mesh::LineIntersection:
-  // 1e-5 < t < 1, src/Mesh.cpp:65)
-  uint32_t i = b;
-  bool blocked = false;
-  while (i < end) {
+  float t;
+  ++c.tris;
+  uint32_t i = b + 1;
+  bool blocked = mt_intersect(A0, B0, C0, o, sdir, t) && t > 1e-5f && t < 1.0f;
+  // the rest two entries per step, both loaded before the first test; each
+  // carries its triangle's test data (Mesh::LineIntersection: 1e-5 < t <
+  // 1, src/Mesh.cpp:65)
+  while (!blocked && i < end) {
     const float4* E0 = S.vis_entries + (size_t)kVisEntryVecs * i;
     const bool has1 = i + 1 < end;
     const float4* E1 = has1 ? E0 + kVisEntryVecs : E0;
-    const float4 A0 = __ldg(E0), B0 = __ldg(E0 + 1), C0 = __ldg(E0 + 2);
-    const float4 A1 = __ldg(E1), B1 = __ldg(E1 + 1), C1 = __ldg(E1 + 2);
-    if (check && A0.w > cut) break;
-    const bool use1 = has1 && !(check && A1.w > cut);
-    float t;
-    ++c.tris;
-    ++i;
-    if (mt_intersect(A0, B0, C0, o, sdir, t) && t > 1e-5f && t < 1.0f) {
-      blocked = true;
-      break;
-    }
-    if (!use1) break;
+    const float4 A1 = __ldg(E0), B1 = __ldg(E0 + 1), C1 = __ldg(E0 + 2);
+    const float4 A2 = __ldg(E1), B2 = __ldg(E1 + 1), C2 = __ldg(E1 + 2);
+    if (check && A1.w > cut) break;
+    const bool use2 = has1 && !(check && A2.w > cut);
     ++c.tris;
     ++i;
     if (mt_intersect(A1, B1, C1, o, sdir, t) && t > 1e-5f && t < 1.0f) {
       blocked = true;
       break;
     }
+    if (!use2) break;
+    ++c.tris;
+    ++i;
+    if (mt_intersect(A2, B2, C2, o, sdir, t) && t > 1e-5f && t < 1.0f) blocked = true;
   }
   c.map += i - b;
   return blocked ? 1 : 0;

@@ -235,18 +235,29 @@ __global__ void k_vis_pack(const uint64_t* __restrict__ keys, const int32_t* __r
   E[2] = make_float4(C.x, C.y, C.z, 0.0f);
 }
 
-// Cell c: (start, end, the distances of its first kVisCellDists entries,
-// +inf past the end); start = the binary-searched first entries.
+// Cell c: (start, end, d1, d2) and its first entry with d0 (see VisMap);
+// start = the binary-searched first entries, entries[] already packed.
 __global__ void k_vis_cells(const uint32_t* __restrict__ start, const uint64_t* __restrict__ keys,
-                            uint64_t cells, float4* __restrict__ out) {
+                            const float4* __restrict__ entries, uint64_t cells,
+                            float4* __restrict__ out) {
   const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cells) return;
   const uint32_t b = start[c], e = start[c + 1];
-  float d[kVisCellDists];
-  for (int k = 0; k < kVisCellDists; ++k)
-    d[k] = b + k < e ? __uint_as_float((uint32_t)keys[b + k]) : __int_as_float(0x7f800000);
-  out[2 * c] = make_float4(__uint_as_float(b), __uint_as_float(e), d[0], d[1]);
-  out[2 * c + 1] = make_float4(d[2], d[3], d[4], d[5]);
+  const float inf = __int_as_float(0x7f800000);
+  const float d1 = b + 1 < e ? __uint_as_float((uint32_t)keys[b + 1]) : inf;
+  const float d2 = b + 2 < e ? __uint_as_float((uint32_t)keys[b + 2]) : inf;
+  float4* o = out + 4 * c;
+  o[0] = make_float4(__uint_as_float(b), __uint_as_float(e), d1, d2);
+  if (b < e) {
+    const float4* E = entries + (size_t)kVisEntryVecs * b;
+    o[1] = E[0];
+    o[2] = E[1];
+    o[3] = E[2];
+  } else {
+    o[1] = make_float4(0.0f, 0.0f, 0.0f, inf);
+    o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    o[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
 }
 
 int bits_for(uint64_t v) {
@@ -360,13 +371,14 @@ cudaError_t build_vis_map(const DeviceScene& s, const float (*locs)[3], int nrec
     VCK(cudaMalloc(&out->entries, kVisEntryBytes * (size_t)std::max<int64_t>(n, 1)));
     k_vis_start<<<(unsigned)((cells + 1 + B - 1) / B), B, 0, st>>>(dk.Current(), n, cells, start);
     VCK(cudaGetLastError());
-    k_vis_cells<<<(unsigned)((cells + B - 1) / B), B, 0, st>>>(start, dk.Current(), cells, out->cells);
-    VCK(cudaGetLastError());
     if (n > 0) {
       k_vis_pack<<<(unsigned)((n + B - 1) / B), B, 0, st>>>(dk.Current(), dv.Current(), n, s.tris,
                                                              (int)s.num_tris, out->entries);
       VCK(cudaGetLastError());
     }
+    k_vis_cells<<<(unsigned)((cells + B - 1) / B), B, 0, st>>>(start, dk.Current(), out->entries,
+                                                               cells, out->cells);
+    VCK(cudaGetLastError());
     VCK(cudaStreamSynchronize(st));
     out->res = res;
     out->num_recs = nrec;
