@@ -281,6 +281,9 @@ def ref_render_lib():
         R.ref_render_band.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
                                       C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p]
+        R.ref_calc_t60.restype = C.c_int
+        R.ref_calc_t60.argtypes = [C.c_char_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]
         R.ref_last_error.restype = C.c_char_p
         lib().oracle_random_tape.restype = C.c_int
         lib().oracle_random_tape.argtypes = [C.POINTER(N.EarSceneDesc), C.POINTER(N.EarSource),
@@ -342,9 +345,10 @@ def grouped_by_material(w):
     return w.vertices[order], w.material_ids[order]
 
 
-def write_reference_scene(w, directory) -> Path:
+def write_reference_scene(w, directory, samples=1000) -> Path:
     """Writes `w` as scene.ear (with a short silent dry.wav beside it, named
-    by its full path as the Blender exporter writes it) into `directory`."""
+    by its full path as the Blender exporter writes it, and `samples` in its
+    settings) into `directory`."""
     import wave
 
     from ear_gb300 import earfile
@@ -358,7 +362,7 @@ def write_reference_scene(w, directory) -> Path:
         f.setframerate(44100)
         f.writeframes(np.zeros(64, np.int16).tobytes())
     ear = d / "scene.ear"
-    ear.write_bytes(earfile.workload_to_ear(w, samples=1000, source_file=str(wav.resolve())))
+    ear.write_bytes(earfile.workload_to_ear(w, samples=int(samples), source_file=str(wav.resolve())))
     return ear
 
 
@@ -393,3 +397,27 @@ def reference_render(w, directory, num_rays, window, bands=(0, 1, 2)):
         out["tape"][b] = len(tape)
         out["used"][b] = used
     return out
+
+
+def reference_calc_t60(w, directory, samples, window):
+    """The reference's `EAR calc T60` (src/EAR.cpp:55-284: the mid band of
+    the first source at samples / 10 rays, post-processed, T60 of recorder 0
+    track 0, Sabine and Norris-Eyring on the first mesh) on workload `w`,
+    with the oracle's random tape for those rays.  Returns dict(t60 =
+    (ear, sabine, eyring) float32, num_rays, tape, used)."""
+    R = ref_render_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libear_ref_render.so is not built")
+    V, M = grouped_by_material(w)
+    ear = write_reference_scene(w, directory, samples=samples)
+    rays = int(samples) // 10
+    kw = reference_pin_params(w, rays, window)
+    tape = np.ascontiguousarray(
+        random_tape(V, M, w.materials, w.source, w.recorders, band=1, **kw), np.float32)
+    used = C.c_int64(0)
+    nr = C.c_int32(0)
+    out = np.zeros(3, np.float32)
+    if R.ref_calc_t60(str(ear).encode(), tape.ctypes.data, tape.size, C.byref(used), C.byref(nr),
+                      out.ctypes.data) != 0:
+        raise RuntimeError("reference calc T60: " + R.ref_last_error().decode())
+    return {"t60": out, "num_rays": nr.value, "tape": tape.size, "used": used.value}

@@ -6,7 +6,9 @@ SHA-256 of the float32 track over the window, its energy and the energy
 of 64 equal time blocks.  The oracle must reproduce the digests bit for
 bit (tests/test_ref_pin.py) and the GPU's exact kernels the energies
 within 1e-5 (tests/test_gpu_parity.py), where the reference tree is
-absent.
+absent.  It also holds the reference's `EAR calc T60` results (T60 from
+the rendered response, Sabine, Norris-Eyring) on the scenes of
+test_ref_pin.T60_CASES, as float32 bit patterns.
 
     python tests/golden/make_reference_golden.py [--reference REFERENCE_ROOT]
 
@@ -53,7 +55,7 @@ def main():
     import oracle
 
     sys.path.insert(0, str(ROOT / "tests"))
-    from test_ref_pin import CASES
+    from test_ref_pin import CASES, T60_CASES
 
     cases = []
     for name, rays, window in FIXTURE:
@@ -74,10 +76,21 @@ def main():
             tracks.append(row)
         cases.append({"name": name, "rays": rays, "window": window, "tape": r["tape"],
                       "tracks": tracks})
+    t60 = []
+    for name in sorted(T60_CASES):
+        make, samples, window = T60_CASES[name]
+        with tempfile.TemporaryDirectory() as d:
+            r = oracle.reference_calc_t60(make(), d, samples, window)
+        t60.append({"name": name, "samples": samples, "window": window,
+                    "t60_bits": [int(x) for x in r["t60"].view(np.uint32)],
+                    "t60": [float(x) for x in r["t60"]]})
     out = {"what": "the reference's own Scene::Render (src/Scene.cpp:111-318) compiled from its "
                    "sources with a GMTL/Boost interface shim, on the oracle's random tape; "
                    "max 1000 path vertices, cut-off 1e-8, point source, static",
-           "cases": cases}
+           "cases": cases,
+           "calc_t60_what": "the `EAR calc T60` branch of src/EAR.cpp:55-284 on the same build: "
+                            "(T60_ear, T60_sabine, T60_eyring)",
+           "calc_t60": t60}
     (HERE / "reference_render.json").write_text(json.dumps(out, indent=1))
     print("wrote", HERE / "reference_render.json")
 

@@ -96,3 +96,64 @@ def test_oracle_equals_reference_fixture():
                 assert _track_digest(o["hist32"][t, b]) == ref["sha256"], (case["name"], t, b)
                 assert int(o["first_sample"][t, b]) == ref["first_sample"]
                 assert int(o["last_sample"][t, b]) == min(ref["real_length"], window)
+
+
+T60_CASES = {
+    # name: (workload, samples in the settings block (samples / 10 rays), window)
+    "shoebox": (scenes.shoebox, 600, 88200),
+    "small_test_room": (scenes.small_test_room, 600, 44100),
+}
+
+
+def _calc_t60_from_oracle(w, rays, window):
+    """`EAR calc T60` from this library's post-processing and statistics
+    (the calls the command line makes) on the oracle's mid-band render."""
+    import ctypes as C
+
+    from ear_gb300 import _native as N, post
+
+    V, M = oracle.grouped_by_material(w)
+    kw = oracle.reference_pin_params(w, rays, window)
+    o = oracle.render(V, M, w.materials, w.source, w.recorders, threads=1,
+                      **dict(kw, bands=(1,)))
+    t_ear = post.calc_t60(o["hist32"][:, 1], o["first_sample"][:, 1], o["last_sample"][:, 1],
+                          tracks_per_recorder=[r.tracks for r in w.recorders])
+    ids, counts = np.unique(M, return_counts=True)  # one MESH block per material
+    blocks = counts.astype(np.int64)
+    mat = w.materials[int(ids[0])].to_c()
+    stats = np.zeros(5, np.float32)
+    air_mid = float(np.float32(w.render.get("air_absorption", (0.0, 0.0, 0.0))[1]))
+    N.check(N.lib().ear_statistical_t60(np.ascontiguousarray(V, np.float32).ctypes.data,
+                                        blocks.ctypes.data, len(blocks), C.byref(mat), air_mid,
+                                        stats.ctypes.data))
+    return np.array([t_ear, stats[3], stats[4]], np.float32)
+
+
+@pytest.mark.parametrize("name", sorted(T60_CASES))
+def test_reference_calc_t60_equals_library(name, tmp_path):
+    """The reference's `EAR calc T60` branch (src/EAR.cpp:55-284) -- its
+    render, Recorder::Power / Truncate, RecorderTrack::T60 and the Sabine /
+    Norris-Eyring formulas on Mesh::Volume / Area / TotalAbsorption /
+    AverageAbsorption -- gives the same three floats, bit for bit, as this
+    library's post-processing and statistics on the oracle's render."""
+    _ref_lib()
+    make, samples, window = T60_CASES[name]
+    w = make()
+    ref = oracle.reference_calc_t60(w, tmp_path, samples, window)
+    assert ref["num_rays"] == samples // 10
+    assert ref["used"] == ref["tape"] > 0
+    ours = _calc_t60_from_oracle(w, samples // 10, window)
+    assert ref["t60"][0] > 0 and ref["t60"][1] > 0 and ref["t60"][2] > 0
+    np.testing.assert_array_equal(ref["t60"].view(np.uint32), ours.view(np.uint32))
+
+
+def test_library_calc_t60_equals_reference_fixture():
+    """Runs everywhere: the library's post-processing and statistics on the
+    oracle's render give the reference's `EAR calc T60` floats recorded in
+    the fixture, bit for bit."""
+    g = json.loads(GOLDEN.read_text())
+    assert {c["name"] for c in g["calc_t60"]} == set(T60_CASES)
+    for case in g["calc_t60"]:
+        make, _, _ = T60_CASES[case["name"]]
+        ours = _calc_t60_from_oracle(make(), case["samples"] // 10, case["window"])
+        assert ours.view(np.uint32).tolist() == case["t60_bits"], case["name"]
