@@ -407,11 +407,11 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     if (hit) {
       int kb = -1;
       float best = 0.0f;
-#pragma unroll
       // nearest hit child first; visibility tests in scenes where most
       // segments are blocked go farthest first (occluders between the
       // surface and the listener are met sooner)
       const bool far = ANY && S.any_far;
+#pragma unroll
       for (int k = 0; k < 4; ++k)
         if (((hit >> k) & 1u) && (kb < 0 || (far ? tk[k] > best : tk[k] < best))) {
           best = tk[k];
