@@ -101,7 +101,7 @@ struct __align__(16) SceneRef {
   int any_far;  // visibility tests visit the farthest hit child first
   // listener visibility maps of the recorders (vis_res = 0: none); a cell
   // holding more than vis_cap entries is left to the tree traversal
-  const float4* vis_cells;    // 2 float4 per cell (VisMap)
+  const float4* vis_cells;    // 4 float4 (64 bytes) per cell (VisMap)
   const float4* vis_entries;  // kVisEntryVecs float4 per entry
   int vis_res;
   int vis_cap;
@@ -209,11 +209,11 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
                        cudaStream_t stream, char* err, size_t errlen);
 
 // Listener visibility maps (vismap.cu): per recorder, a cube map of
-// res x res cells per face around its location; cell c lists, from
-// entries[start[c]] to entries[start[c+1]], (leaf position, distance bits)
-// of the triangles whose padded box meets the cell's cone of directions,
-// nearest first.  Cell index: ((recorder * 6 + face) * res + iv) * res + iu,
-// face = 2 * major axis + (major component < 0).
+// res x res cells per face around its location; cell c lists the triangles
+// whose padded box meets the cell's cone of directions, nearest first (by
+// the distance of the padded box from the recorder), as the entries from
+// its cell's start to its end.  Cell index: ((recorder * 6 + face) * res +
+// iv) * res + iu, face = 2 * major axis + (major component < 0).
 // A visibility-list entry carries its triangle's test data inline, so a
 // walk reads one array: float4 (v0, distance bits of the padded box from
 // the recorder), float4 (e1 = v1 - v0, leaf position bits), float4 (e2 =
