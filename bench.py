@@ -777,7 +777,10 @@ def run_ours(args):
                   "roofline": roofline_of(tr_, rs, hbm, src, l2,
                                           TRAFFIC_PER_LAUNCH.get((wr.name, int(kr["num_rays"])))),
                   "entries_read_per_segment":
-                      tr_["agg"]["map_entries"] / max(1, tr_["agg"]["segments"])}
+                      tr_["agg"]["map_entries"] / max(1, tr_["agg"]["segments"]),
+                  "per_segment": {k: tr_["agg"][k] / max(1, tr_["agg"]["segments"])
+                                  for k in ("node_visits", "triangle_tests", "splat_bins",
+                                            "map_entries")}}
         launches += 3 * rs
 
     acc = None
@@ -819,6 +822,14 @@ def run_ours(args):
                "rays_per_s": agg["rays"] / (t["total_ms"] / 1000.0) * world}
         # tree quality beside segments/s (unit node and triangle costs)
         run["bvh"]["sah_cost"] = {"binary": tracer.sah_cost(2), "wide4": tracer.sah_cost(4)}
+        # the device-counted units of the algorithmic bytes, per segment
+        # (a 4-wide node visit counts two 64-byte halves)
+        nseg = max(1, agg["segments"])
+        run["per_segment"] = {"node_visits_64B": agg["node_visits"] / nseg,
+                              "triangle_tests": agg["triangle_tests"] / nseg,
+                              "splat_bins": agg["splat_bins"] / nseg,
+                              "map_entries": agg["map_entries"] / nseg,
+                              "algorithmic_bytes": alg_bytes(agg) / nseg}
         # listener visibility maps (built during warm-up, reused by the
         # timed steps like the tree; e2e builds them inside every step)
         run["visibility_map"] = {"setting": args.vismap, "build_ms": t["map_build_ms"],
