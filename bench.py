@@ -780,8 +780,8 @@ def run_ours(args):
                       tr_["agg"]["map_entries"] / max(1, tr_["agg"]["segments"]),
                   "per_segment": {k: tr_["agg"][k] / max(1, tr_["agg"]["segments"])
                                   for k in ("node_visits", "triangle_tests", "splat_bins",
-                                            "map_entries")}}
-        launches += 3 * rs
+                                            "map_entries")},
+                  "gpu_launches": 3 * rs}
 
     acc = None
     if not args.no_accuracy:
