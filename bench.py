@@ -565,12 +565,12 @@ def auralisation(device: int, steps: int, cpu: bool):
 # dram__bytes_write.sum) from ncu captures of the fast kernels with the
 # automatic visibility maps, keyed by (workload, rays per band); other
 # settings report null.  The cathedral figure is a capture at 1e6 rays per
-# band (277.5 GB for 9.979e7 segments) scaled to the 1e8-ray launch by the
-# segments rendered (9.977e9): the traffic of a persistent launch grows
+# band (265.1 GB for 9.979e7 segments) scaled to the 1e8-ray launch by the
+# segments rendered (9.978e9): the traffic of a persistent launch grows
 # with the paths it traces.
 TRAFFIC_PER_LAUNCH = {
     ("relief-hall-20k-stereo", 10_000_000): 17_028_675_584,
-    ("cathedral-2M-stereo+8mono", 100_000_000): 27_742_955_983_705,
+    ("cathedral-2M-stereo+8mono", 100_000_000): 26_507_513_248_521,
 }
 
 
@@ -879,7 +879,7 @@ def main():
     ap.add_argument("--width", type=int, default=0, choices=[0, 2, 4],
                     help="BVH traversal width (0: by scene size)")
     ap.add_argument("--vismap", type=int, default=0,
-                    help="listener visibility maps: 0 automatic, -1 off, 8..2048 cells per face edge")
+                    help="listener visibility maps: 0 automatic, -1 off, 8..4096 cells per face edge")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

@@ -298,8 +298,8 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   const int order = opts ? opts->visibility_order : 0;
   if (order < 0 || order > 2) return fail(EAR_ERR_INVALID_ARG, "visibility_order must be 0, 1 or 2");
   const int vmap = opts ? opts->visibility_map : 0;
-  if (vmap < -1 || (vmap > 0 && (vmap < 8 || vmap > 2048)))
-    return fail(EAR_ERR_INVALID_ARG, "visibility_map must be -1, 0 or 8..2048");
+  if (vmap < -1 || (vmap > 0 && (vmap < 8 || vmap > 4096)))
+    return fail(EAR_ERR_INVALID_ARG, "visibility_map must be -1, 0 or 8..4096");
   cudaError_t e = build_lbvh(s->ds, pad, max_leaf, builder == EAR_BVH_PLOC ? kBuilderPloc : kBuilderLbvh,
                              radius, 0, msg, sizeof msg);
   // the triangles' leaf order changed: the visibility maps address them

@@ -181,7 +181,7 @@ class Tracer:
         """(Re)build the BVH: builder "default", "lbvh" or "ploc"; traversal
         width 2, 4 or 0 (4-wide from 4096 triangles); visibility_order 1
         nearest first, 2 farthest first, 0 automatic; visibility_map -1 off,
-        8..2048 on with that many cells per cube-face edge, 0 automatic
+        8..4096 on with that many cells per cube-face edge, 0 automatic
         (listener visibility maps: visibility tests by direction lists
         around each recorder instead of tree traversals)."""
         opts = N.EarBvhOpts()

@@ -134,9 +134,11 @@ typedef struct ear_bvh_opts {
      render builds them on first use of a recorder set and keeps them until
      the set, the tree or this setting changes; a batch builds one per scene
      over its jobs' recorders.  > 0: on, with this many cells per face edge
-     (8..2048); -1: off; 0 = automatic: built for renders of at least as
-     many rays (times bands) as the scene has triangles, with
-     4 sqrt(triangles) cells per edge (a multiple of 64, 64..2048), lowered
+     (8..4096; refused, the tests left to the tree, when the lists would
+     not fit half the free device memory); -1: off; 0 = automatic: built
+     for renders of at least as many rays (times bands) as the scene has
+     triangles, with 4 sqrt(triangles) cells per edge (a multiple of 64,
+     64..2560), lowered
      while the lists would hold more than EAR_VISMAP_AUTO_MAX_ENTRIES
      entries; used by any render while they match its recorder set.  Never
      changes a result. */

@@ -44,11 +44,11 @@ double gauss() {
 int main(int argc, char** argv) {
   const int cases = argc > 1 ? atoi(argv[1]) : 20000;
   g_state ^= argc > 2 ? (uint64_t)atoll(argv[2]) : 0ull;
-  const int resolutions[4] = {8, 64, 512, 2048};
+  const int resolutions[6] = {8, 64, 512, 2048, 2560, 4096};
   const double sizes[5] = {0.001, 0.02, 0.05, 0.3, 3.0};
   long queries = 0, misses = 0, cut_misses = 0, with_tri = 0;
   for (int c = 0; c < cases; ++c) {
-    const int res = resolutions[c % 4];
+    const int res = resolutions[(c + c / 5) % 6];
     float loc[3];
     for (int k = 0; k < 3; ++k) loc[k] = (float)uni(-30.0, 30.0);
     // triangle centre: a random direction and distance from the recorder,
