@@ -146,6 +146,7 @@ SIGNATURES = {
     "ear_scene_sah_cost": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_float,
                                      C.POINTER(C.c_double)]),
     "ear_scene_set_bvh_width": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ear_scene_bvh_width": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ear_num_tracks": (C.c_int32, [C.POINTER(EarRecorder), C.c_int32]),
     "ear_render": (C.c_int, [C.c_void_p, C.POINTER(EarSource), C.POINTER(EarRecorder), C.c_int32,
                              C.POINTER(EarRenderParams), C.POINTER(EarHistograms),

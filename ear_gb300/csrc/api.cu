@@ -307,7 +307,8 @@ ear_status ear_scene_build_bvh(ear_scene* s, const ear_bvh_opts* opts) {
   s->vis_valid = false;
   ++s->bvh_gen;
   s->vis_opt = vmap;
-  s->ds.wide = width == 4 || (width == 0 && s->ds.num_tris >= kWideFrom);
+  // a 4-wide tree deeper than its traversal trail is not kept (nodes4 null)
+  s->ds.wide = s->ds.nodes4 != nullptr && (width == 4 || (width == 0 && s->ds.num_tris >= kWideFrom));
   s->ds.any_order = order;
   s->ds.any_far = order == 2 ? 1 : 0;
   s->probe_valid = false;
@@ -325,7 +326,17 @@ ear_status ear_scene_set_bvh_width(ear_scene* s, int32_t width) {
   if (!s) return fail(EAR_ERR_INVALID_ARG, "null scene");
   if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
   if (width != 2 && width != 4) return fail(EAR_ERR_INVALID_ARG, "width must be 2 or 4");
+  if (width == 4 && !s->ds.nodes4)
+    return fail(EAR_ERR_STATE, "the scene has no 4-wide tree (deeper than %d levels)", kMaxDepth4);
   s->ds.wide = width == 4;
+  return EAR_OK;
+}
+
+ear_status ear_scene_bvh_width(const ear_scene* s, int32_t* width) {
+  g_err[0] = 0;
+  if (!s || !width) return fail(EAR_ERR_INVALID_ARG, "null argument");
+  if (!s->bvh) return fail(EAR_ERR_STATE, "ear_scene_build_bvh has not been called");
+  *width = s->ds.wide ? 4 : 2;
   return EAR_OK;
 }
 

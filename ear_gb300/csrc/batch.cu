@@ -367,7 +367,8 @@ void cache_store(const char* path, const std::string& key, const ear_batch_confi
 
 ear_status set_width(ear_batch* b, int width) {
   for (ear_scene* s : b->scenes) {
-    const ear_status rc = ear_scene_set_bvh_width(s, width);
+    // a scene without a 4-wide tree (deeper than its trail) stays binary
+    const ear_status rc = ear_scene_set_bvh_width(s, width == 4 && !s->ds.nodes4 ? 2 : width);
     if (rc != EAR_OK) return rc;
   }
   return sync_scenes(b);

@@ -702,6 +702,7 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
     void* st4 = nullptr;
     size_t st4_bytes = 0;
     int levels = 0, nf = 1, base = 0, total = 0;
+    bool too_deep = false;
     const int root_parent = -1, root = 0;
     const int cap = nn > 0 ? nn : 1;  // at most one 4-wide node per binary node
     CK(cudaMalloc(&s.nodes4, sizeof(Node4) * (size_t)cap));
@@ -718,9 +719,12 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
     CK(cudaMemcpyAsync(front, &root, sizeof(int), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(par4, &root_parent, sizeof(int), cudaMemcpyHostToDevice, stream));
     while (nf > 0) {
-      if (++levels > kMaxDepth4 || base + nf > cap) {
-        snprintf(err, errlen, "4-wide BVH deeper than the %d levels of the traversal trail",
-                 kMaxDepth4);
+      if (++levels > kMaxDepth4) {
+        too_deep = true;  // beyond the trail: the binary tree serves the scene
+        break;
+      }
+      if (base + nf > cap) {
+        snprintf(err, errlen, "4-wide BVH larger than its binary tree");
         rc = cudaErrorInvalidValue;
         break;
       }
@@ -752,8 +756,15 @@ cudaError_t build_lbvh(DeviceScene& s, float box_pad, int max_leaf, int builder,
     cudaFree(slots);
     cudaFree(st4);
     if (rc != cudaSuccess) goto done;
-    s.num_nodes4 = total;
-    s.depth4 = levels;
+    if (too_deep) {
+      cudaFree(s.nodes4);
+      s.nodes4 = nullptr;
+      s.num_nodes4 = 0;
+      s.depth4 = 0;
+    } else {
+      s.num_nodes4 = total;
+      s.depth4 = levels;
+    }
   }
   k_gather<<<G, B, 0, stream>>>(s.vertices, s.mat_ids, idx2, n, s.tris);
   CK(cudaGetLastError());

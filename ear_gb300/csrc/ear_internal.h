@@ -29,7 +29,9 @@ struct __align__(32) Node4 {
   int4 child;
   int4 meta;  // x: parent Node4 (-1 at the root), y: mask of occupied slots
 };
-constexpr int kMaxDepth4 = 32;  // levels of the 128-bit traversal trail
+// levels of the 64-bit traversal trail; a deeper 4-wide tree is not kept
+// and the scene traverses its binary tree
+constexpr int kMaxDepth4 = 16;
 
 constexpr int kLeafCountShift = 27;
 constexpr int kLeafStartMask = (1 << kLeafCountShift) - 1;

@@ -179,7 +179,8 @@ class Tracer:
                   ploc_radius: int = 0, width: int = 0, visibility_order: int = 0,
                   visibility_map: int = 0) -> None:
         """(Re)build the BVH: builder "default", "lbvh" or "ploc"; traversal
-        width 2, 4 or 0 (4-wide from 4096 triangles); visibility_order 1
+        width 2, 4 or 0 (4-wide from 4096 triangles; a 4-wide tree deeper
+        than 16 levels is not kept, and the binary tree serves); visibility_order 1
         nearest first, 2 farthest first, 0 automatic; visibility_map -1 off,
         8..4096 on with that many cells per cube-face edge, 0 automatic
         (listener visibility maps: visibility tests by direction lists
@@ -194,7 +195,6 @@ class Tracer:
         opts.visibility_order = int(visibility_order)
         opts.visibility_map = int(visibility_map)
         N.check(N.lib().ear_scene_build_bvh(self._h, C.byref(opts)))
-        self._width = int(width) if width else (4 if self.num_triangles >= 4096 else 2)
         self._builder = builder
 
     @property
@@ -209,7 +209,14 @@ class Tracer:
         return {"triangles": nt.value, "nodes": nn.value, "max_depth": depth.value,
                 "box_pad": pad.value, "device_bytes": db.value,
                 "builder": getattr(self, "_builder", "default"),
-                "width": getattr(self, "_width", 2)}
+                "width": self.width}
+
+    @property
+    def width(self) -> int:
+        """The tree the traversal uses: 2 (binary) or 4."""
+        w = C.c_int32()
+        N.check(N.lib().ear_scene_bvh_width(self._h, C.byref(w)))
+        return w.value
 
     def sah_cost(self, width: int = 4, node_cost: float = 1.0,
                  triangle_cost: float = 1.0) -> float:
@@ -222,7 +229,6 @@ class Tracer:
     def set_width(self, width: int) -> None:
         """Traverse the binary (2) or 4-wide (4) tree; no rebuild."""
         N.check(N.lib().ear_scene_set_bvh_width(self._h, int(width)))
-        self._width = int(width)
 
     def render(self, source: Source, recorders: Sequence[Recorder], *, keyframe: int = -1,
                out=None, **kw) -> RenderResult:

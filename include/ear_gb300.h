@@ -118,7 +118,10 @@ typedef struct ear_bvh_opts {
   /* Tree the traversal uses: 2 (binary), 4 (4-wide, built from the binary
      tree: fewer dependent node loads per query, costlier visits) or 0 =
      4-wide from 4096 triangles on.  Both trees are built; the choice can
-     be changed later with ear_scene_set_bvh_width.  Never changes a result. */
+     be changed later with ear_scene_set_bvh_width.  A 4-wide tree deeper
+     than the 16 levels of its traversal trail is not kept: the scene then
+     traverses its binary tree (ear_scene_bvh_width reports the tree in
+     use).  Never changes a result. */
   int32_t width;
   /* Order of the visibility tests' traversal: 1 nearest hit child first, 2
      farthest first (meets occluders between the surface and the listener
@@ -196,8 +199,13 @@ typedef struct ear_render_params {
 } ear_render_params;
 
 /* Selects the tree the traversal uses (2 or 4, see ear_bvh_opts.width)
-   without rebuilding.  No counterpart in the reference. */
+   without rebuilding; EAR_ERR_STATE for 4 when no 4-wide tree was kept.
+   No counterpart in the reference. */
 ear_status ear_scene_set_bvh_width(ear_scene* scene, int32_t width);
+
+/* The tree the traversal uses: *width = 2 (binary) or 4.  No counterpart
+   in the reference. */
+ear_status ear_scene_bvh_width(const ear_scene* scene, int32_t* width);
 
 /* Per-render statistics (counted on the device). */
 typedef struct ear_render_stats {
@@ -347,7 +355,8 @@ typedef struct ear_batch_config {
                              set by ear_batch_tune (read-only otherwise) */
   int32_t no_graph;       /* 1: launch directly instead of replaying the
                              captured CUDA graph */
-  int32_t bvh_width;      /* tree width the batch's scenes traverse (2 or 4);
+  int32_t bvh_width;      /* tree width the batch's scenes traverse (2 or 4:
+                             the 4-wide tree of every scene that kept one);
                              set by ear_batch_tune, 0 = the scenes' own */
   int32_t reserved[3];
 } ear_batch_config;

@@ -196,6 +196,45 @@ def test_empty_and_single_triangle_scene():
         _check_render(w2, 500)
 
 
+def _chain_scene(n=60):
+    """n unit triangles in the planes x = 2^k: each is nearest to the cluster
+    of all smaller ones, so PLOC builds a chain of depth n - 1 (within the
+    62 levels of the binary trail) whose 4-wide collapse (three binary
+    levels per node) is deeper than the 16 levels of the 4-wide trail."""
+    from ear_gb300 import Recorder
+
+    w = scenes.small_test_room()
+    x = np.float32(2.0) ** np.arange(n, dtype=np.float32)
+    v = np.zeros((n, 9), np.float32)
+    v[:, 0::3] = x[:, None]
+    v[:, 4] = 1.0  # (x, 0, 0), (x, 1, 0), (x, 0, 1)
+    v[:, 8] = 1.0
+    return scenes.Workload(name="chain", vertices=v, material_ids=np.zeros(n, np.int32),
+                           materials=w.materials[:1],
+                           source=Source(location=np.array([1.5, 0.3, 0.3], np.float32)),
+                           recorders=[Recorder(location=np.array([1.5, 2.0, 2.0], np.float32))],
+                           render=dict(w.render, bands=(0, 1, 2)))
+
+
+def test_deep_tree_keeps_the_binary_traversal():
+    """A 4-wide tree deeper than its 64-bit trail is not kept: the scene
+    traverses its binary tree, bit-exact with the oracle, and asking for the
+    4-wide tree is refused."""
+    from ear_gb300._native import EarError
+
+    w = _chain_scene()
+    with _tracer(w, width=4) as tr:
+        assert tr.info()["width"] == 2 and tr.info()["max_depth"] > 48
+        with pytest.raises(EarError):
+            tr.set_width(4)
+        with pytest.raises(EarError):
+            tr.sah_cost(4)
+    with _tracer(scenes.small_test_room(), width=4) as tr:
+        assert tr.info()["width"] == 4
+    _check_debug(w, 2000, 20, width=4)
+    _check_render(w, 2000, width=4)
+
+
 def test_device_output_tensor():
     torch = pytest.importorskip("torch")
     w = scenes.small_test_room()
