@@ -341,7 +341,9 @@ __device__ bool traverse2(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
 // counter is kept; a lane's error flags are sticky, so no copy of them
 // either: the two registers saved reduce the bounce kernel's spills, +5.2%
 // segments/s on the nave and +6.6% on the hall.  (The same two changes in
-// the binary traversal cost the small rooms 20-28%: not made there.)
+// the binary traversal cost the small rooms 20-28%: not made there.)  The
+// node visits are counted once, from the budget spent, at the end (+1.8%
+// on the nave).
 //
 // A node visit tests its candidate slots' boxes,
 // tests hit leaf children at once (one merged loop) and descends into the
@@ -369,7 +371,9 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
   int cur = 0;
   unsigned long long tlo = 0ull;  // the trail (all zero: nothing pending)
   bool reentry = false;  // cur's own pending mask is the low nibble
-  int budget = S.traverse_budget;  // node visits and climbs left
+  // node visits left; the climbs need no budget: each drops a nibble of
+  // the trail, so a dead end climbs at most 16 levels
+  int budget = S.traverse_budget;
   bool blocked = false;
   for (;;) {
     if (--budget < 0) {
@@ -378,7 +382,6 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
     }
     cur = clamp_index(cur, S.num_nodes, err);
     const Node4* nd = nodes + cur;
-    c.nodes += 2;  // two 64-byte halves
     // the near and far planes of each axis, picked by the load address
     // (lox, hix, loy, hiy, loz, hiz are consecutive float4s)
     const float4* P = &nd->lox;
@@ -454,15 +457,13 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
         done = true;
         break;
       }
-      if (--budget < 0) {
-        err |= kErrBudget;
-        done = true;
-        break;
-      }
       par = __ldg(&nodes[cur].meta.x);
     }
     if (done) break;
   }
+  // node visits = budget spent (the climbs are bounded by the trail:
+  // each step drops a nibble); two 64-byte halves each
+  c.nodes += 2u * (uint32_t)(S.traverse_budget - budget);
   if (err) {  // any error of this lane invalidates its results
     h.pos = -1;
     return false;
