@@ -66,7 +66,7 @@ class EarRenderParams(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("context", C.c_uint32), ("bands_mask", C.c_uint32),
                 ("num_rays", C.c_uint64), ("max_bounces", C.c_int32), ("num_bins", C.c_int32),
                 ("cutoff", C.c_double), ("air_absorption", F3), ("dry_level", C.c_float),
-                ("flags", C.c_uint32), ("reserved0", C.c_int32), ("stream", C.c_void_p),
+                ("flags", C.c_uint32), ("traverse_budget", C.c_int32), ("stream", C.c_void_p),
                 ("first_ray", C.c_uint64)]
 
 

@@ -470,7 +470,10 @@ ear_status choose_visibility_order(ear_scene* s, const ear_recorder* recs, int32
     constexpr int kProbeSegments = 4096;
     if (!s->probe) CU(cudaMalloc(&s->probe, sizeof(unsigned)));
     CU(cudaMemsetAsync(s->probe, 0, sizeof(unsigned), st));
-    CU(ops->probe(a, kProbeSegments, s->probe, st));
+    // the cached order must not depend on a caller's traversal budget
+    TraceArgs pa = a;
+    pa.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
+    CU(ops->probe(pa, kProbeSegments, s->probe, st));
     unsigned blocked = 0;
     CU(cudaMemcpyAsync(&blocked, s->probe, sizeof blocked, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
@@ -590,6 +593,7 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   if (p->num_bins <= 0 || p->num_bins > (1 << 30)) return fail(EAR_ERR_INVALID_ARG, "bad num_bins");
   if (bands_mask == 0 || (bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
   if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
+  if (p->traverse_budget < 0) return fail(EAR_ERR_INVALID_ARG, "negative traverse_budget");
   if (p->num_rays > (1ull << 47) || p->first_ray > (1ull << 47) - p->num_rays)
     return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   if (src->num_emitter_triangles < 0 || (src->num_emitter_triangles > 0 && !src->emitter_vertices))
@@ -630,7 +634,9 @@ ear_status prepare(ear_scene* s, const ear_source* src, const ear_recorder* recs
   a.num_bins = p->num_bins;
   a.stride = (p->num_bins + 3) & ~3;
   a.num_tracks = tracks;
-  a.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
+  a.traverse_budget = p->traverse_budget > 0 ? p->traverse_budget
+                                             : traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes,
+                                                               s->ds.wide != 0);
   a.dbg_band = -1;
   out->num_tracks = tracks;
 
@@ -1155,6 +1161,7 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
     return fail(EAR_ERR_INVALID_ARG, "ear_render_noalloc: hist must be 16-byte aligned");
   if (p->bands_mask == 0 || (p->bands_mask & ~7u)) return fail(EAR_ERR_INVALID_ARG, "bad bands_mask");
   if (p->max_bounces < 0) return fail(EAR_ERR_INVALID_ARG, "negative max_bounces");
+  if (p->traverse_budget < 0) return fail(EAR_ERR_INVALID_ARG, "negative traverse_budget");
   if (p->num_rays > (1ull << 47) || p->first_ray > (1ull << 47) - p->num_rays)
     return fail(EAR_ERR_INVALID_ARG, "first_ray + num_rays above 2^47");
   DevRecorder dr[kMaxRecorders];
@@ -1205,7 +1212,9 @@ extern "C" ear_status ear_render_noalloc(ear_scene* s, const ear_source* src,
   a.direct_vis = direct ? reinterpret_cast<int*>(scratch + kNaVis) : nullptr;
   a.counters = reinterpret_cast<unsigned long long*>(scratch + kNaCounters);
   a.error_flag = reinterpret_cast<int*>(scratch + kNaError);
-  a.traverse_budget = traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes, s->ds.wide != 0);
+  a.traverse_budget = p->traverse_budget > 0 ? p->traverse_budget
+                                             : traverse_budget(s->ds.wide ? s->ds.num_nodes4 : s->ds.num_nodes,
+                                                               s->ds.wide != 0);
   a.dbg_band = -1;
   // listener visibility maps an earlier ear_render built for this recorder
   // set are read; none is built here (a build allocates)

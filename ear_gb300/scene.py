@@ -113,7 +113,7 @@ def recorders_at(recorders: Sequence[Recorder], keyframe: int):
 def make_params(*, seed=0, context=0, bands=(0, 1, 2), num_rays=1000, max_bounces=N.EAR_REFERENCE_MAX_BOUNCES,
                 num_bins=3 * N.SAMPLE_RATE, cutoff=N.EAR_REFERENCE_CUTOFF, air_absorption=(0.0, 0.0, 0.0),
                 dry=1.0, exact=False, raw=False, no_direct=False, stream=None,
-                first_ray=0) -> N.EarRenderParams:
+                first_ray=0, traverse_budget=0) -> N.EarRenderParams:
     p = N.EarRenderParams()
     p.seed = int(seed)
     p.context = int(context) & 0xFFFFFFFF
@@ -131,6 +131,7 @@ def make_params(*, seed=0, context=0, bands=(0, 1, 2), num_rays=1000, max_bounce
         (N.EAR_FLAG_NO_DIRECT if no_direct else 0)
     p.stream = stream
     p.first_ray = int(first_ray)
+    p.traverse_budget = int(traverse_budget)
     return p
 
 

@@ -188,7 +188,12 @@ typedef struct ear_render_params {
   float air_absorption[3]; /* 'absorption' setting: factor = 1 - a (EAR.cpp:180) */
   float dry_level;         /* 'drylevel' setting */
   uint32_t flags;          /* EAR_FLAG_* */
-  int32_t reserved0;
+  int32_t traverse_budget; /* node visits one BVH traversal may make; a
+                              traversal that needs more stops, and the call
+                              returns EAR_ERR_DEVICE_BUDGET once the launch
+                              has ended (the kernel never waits unbounded).
+                              0 = automatic: 8 x tree nodes + 64, more than
+                              any traversal of a valid tree makes */
   void* stream;            /* cudaStream_t, NULL = default stream */
   uint64_t first_ray;      /* index of this call's first ray: rays
                               first_ray .. first_ray + num_rays - 1 are traced
