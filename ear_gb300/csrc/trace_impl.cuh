@@ -403,33 +403,40 @@ __device__ bool traverse4(const SceneRef& S, V3 o, V3 d, float tlimit, float sla
       if (((cand >> k) & 1u) && b) hit |= 1u << k;
       if (lane4(ch, k) < 0) leaf |= 1u << k;
     }
+    // the next internal child is chosen before the leaf tests, so the
+    // entry distances are dead while the triangles are tested: nearest hit
+    // child first; visibility tests in scenes where most segments are
+    // blocked go farthest first (occluders between the surface and the
+    // listener are met sooner)
+    const unsigned inner = hit & ~leaf;
+    unsigned rest = 0u;
+    int next = 0;
+    if (inner) {
+      int kb = -1;
+      float best = 0.0f;
+      const bool far = ANY && S.any_far;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (((inner >> k) & 1u) && (kb < 0 || (far ? tk[k] > best : tk[k] < best))) {
+          best = tk[k];
+          kb = k;
+        }
+      rest = inner & ~(1u << kb);
+      next = lane4(ch, kb);
+    }
     // hit leaf children, one merged loop
     for (unsigned lm = hit & leaf; lm; lm &= lm - 1u) {
       const int k = __ffs(lm) - 1;
       blocked |= leaf_test<ANY>(S, lane4(ch, k), o, d, h, c, err);
     }
     if (ANY && blocked) break;
-    hit &= ~leaf;
-    if (hit) {
-      int kb = -1;
-      float best = 0.0f;
-      // nearest hit child first; visibility tests in scenes where most
-      // segments are blocked go farthest first (occluders between the
-      // surface and the listener are met sooner)
-      const bool far = ANY && S.any_far;
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (((hit >> k) & 1u) && (kb < 0 || (far ? tk[k] > best : tk[k] < best))) {
-          best = tk[k];
-          kb = k;
-        }
-      const unsigned rest = hit & ~(1u << kb);
+    if (inner) {
       if (reentry) {
         tlo = (tlo & ~0xFull) | rest;
       } else {
         tlo = (tlo << 4) | rest;
       }
-      cur = lane4(ch, kb);
+      cur = next;
       reentry = false;
       continue;
     }
