@@ -196,6 +196,31 @@ def test_empty_and_single_triangle_scene():
         _check_render(w2, 500)
 
 
+def test_render_exact_at_the_recorder_limit():
+    """32 recorders (16 stereo, 16 mono: 48 tracks), the most a render takes,
+    equal the oracle; a 33rd is rejected before any device work."""
+    from ear_gb300 import Recorder
+    from ear_gb300._native import EarError
+
+    w = scenes.small_test_room()
+    rng = np.random.default_rng(32)
+    lo, hi = w.vertices.reshape(-1, 3).min(0), w.vertices.reshape(-1, 3).max(0)
+    recs = []
+    for i in range(32):
+        loc = (lo + (hi - lo) * rng.uniform(0.2, 0.8, 3)).astype(np.float32)
+        if i % 2:
+            recs.append(Recorder(location=loc))
+        else:
+            recs.append(Recorder(location=loc, channels=2,
+                                 right_ear=(loc + np.float32([0.0, -1.0, 0.0])).astype(np.float32),
+                                 head_size=0.18))
+    w.recorders = recs
+    _check_render(w, 600)
+    with _tracer(w) as tr:
+        with pytest.raises(EarError):
+            tr.render(w.source, recs + recs[:1], exact=True, **_kw(w, num_rays=10))
+
+
 def _chain_scene(n=60):
     """n unit triangles in the planes x = 2^k: each is nearest to the cluster
     of all smaller ones, so PLOC builds a chain of depth n - 1 (within the
