@@ -141,7 +141,7 @@ typedef struct ear_bvh_opts {
      not fit half the free device memory); -1: off; 0 = automatic: built
      for renders of at least as many rays (times bands) as the scene has
      triangles, with 4 sqrt(triangles) cells per edge (a multiple of 64,
-     64..2560), lowered
+     64..2816), lowered
      while the lists would hold more than EAR_VISMAP_AUTO_MAX_ENTRIES
      entries; used by any render while they match its recorder set.  Never
      changes a result. */
