@@ -565,12 +565,12 @@ def auralisation(device: int, steps: int, cpu: bool):
 # dram__bytes_write.sum) from ncu captures of the fast kernels with the
 # automatic visibility maps, keyed by (workload, rays per band); other
 # settings report null.  The cathedral figure is a capture at 1e6 rays per
-# band (262.1 GB for 9.979e7 segments) scaled to the 1e8-ray launch by the
+# band (256.9 GB for 9.979e7 segments) scaled to the 1e8-ray launch by the
 # segments rendered (9.978e9): the traffic of a persistent launch grows
 # with the paths it traces.
 TRAFFIC_PER_LAUNCH = {
-    ("relief-hall-20k-stereo", 10_000_000): 16_085_008_384,
-    ("cathedral-2M-stereo+8mono", 100_000_000): 26_201_387_527_683,
+    ("relief-hall-20k-stereo", 10_000_000): 16_081_281_024,
+    ("cathedral-2M-stereo+8mono", 100_000_000): 25_685_502_702_342,
 }
 
 
