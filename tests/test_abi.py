@@ -119,3 +119,22 @@ def test_batch_arguments_are_checked_before_device_work():
     assert N.lib().ear_batch_create(None, 0, None, 0, C.byref(p), C.byref(h)) == N.EAR_ERR_INVALID_ARG
     assert N.lib().ear_batch_run(None, None) == N.EAR_ERR_INVALID_ARG
     assert N.lib().ear_batch_tune(None, None, None) == N.EAR_ERR_INVALID_ARG
+
+
+def test_header_is_plain_c():
+    """include/ear_gb300.h compiles as C99 and as C++11 on its own: the
+    boundary holds no C++ or CUDA types, so a C, cgo or ctypes binding can
+    include it."""
+    import shutil
+    import subprocess
+
+    root = Path(__file__).resolve().parent.parent
+    hdr = str(root / "include" / "ear_gb300.h")
+    for cc, std, lang in (("gcc", "-std=c99", "c"), ("g++", "-std=c++11", "c++")):
+        exe = shutil.which(cc)
+        if exe is None:
+            pytest.skip(cc + " not found")
+        r = subprocess.run([exe, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", lang, hdr],
+                           capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+
